@@ -1,0 +1,296 @@
+#!/usr/bin/env python
+"""Benchmark of the narrowband level-set time step on GB300.
+
+Workload (default): 128^3-cell jittered Freudenthal cube (2,146,689 vertices,
+12,582,912 tetrahedra), union of 3 seeded spheres, mean-curvature flow with
+dt = 0.5 h^2, narrowband 6h, 3x3x3-vertex patches (79,507 patches).  A step is
+one time step: seed search, fast-iterative-method redistance of the
+narrowband, narrowband selection, curvature update.
+
+Metric: narrowband vertex-updates per second, one update = one vertex with
+|phi| <= w after the step's redistance.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With --gpus N > 1 (launched by torch.distributed.run) every rank runs an
+independent replica of the workload (the time step does not shard; see
+the design doc); the timed region is bracketed by a barrier and the maximum time
+over ranks is reported.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sci-solver_level-set_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "narrowband vertex-updates/s (curvature flow, 128^3 jittered cube, 3 spheres)"
+UNIT = "vertex-updates/s"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the FIM sweep kernel from the committed ncu
+    summary (profiles/k_fim_sweep_c3.md), or None."""
+    path = os.path.join(ROOT, "profiles", "k_fim_sweep_c3.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def oracle_rate(w, nsteps, warm, threads, precision=32):
+    """CPU oracle (port of the reference's algorithm) on the same workload:
+    `warm` untimed steps then `nsteps` timed steps."""
+    import lsoracle
+
+    ol = lsoracle.OracleLayout(w["dim"], w["xyz"], w["elems"], w["npart"], w["nparts"])
+    kind = lsoracle.UPDATE[w["update"]]
+    p = ol.params(update_kind=kind, dt=w["dt"], bandwidth=w["bandwidth"], curv_coeff=1.0, nthreads=threads,
+                  precision=precision)
+    hist, _, _, s0 = ol.solve(p, w["phi0"], w["vel"], warm, nb_sets=False)
+    phi = hist[-1]
+    # the timed run continues from the warm state (its first step seeds over
+    # all patches, as a fresh reference GenerateData call does)
+    t0 = time.perf_counter()
+    _, _, _, s1 = ol.solve(p, phi, w["vel"], nsteps, nb_sets=False)
+    sec = time.perf_counter() - t0
+    return s1["nb_vertex_updates"] / sec, sec, s1
+
+
+def run_reference_arm(args, w, rank):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    k = min(args.steps, 5)
+    warm = min(args.warmup, 1)
+    rate, sec, st = oracle_rate(w, k, warm, threads)
+    sample = "%d timed steps after %d warm-up step(s) of the full workload, FP32 oracle port, %d threads" % (k, warm, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
+        "warmup": warm, "ms_per_step": 1000.0 * sec / k, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered cube, sphere-union SDF)",
+        "config": {"workload": w["label"], "steps_requested": args.steps},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="cells per side (128 = the benchmark workload)")
+    ap.add_argument("--fp64-flagged", action="store_true", help="precision form")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+
+    import synth
+
+    w = synth.workload("c3", seed=0, n=args.n)
+    w["label"] = "c3 curvature flow %d^3 cells x 6 tets (%d verts, %d tets), w=6h, dt=0.5h^2, 3x3x3-vertex patches" % (
+        w["n"], len(w["xyz"]), len(w["elems"]))
+    if args.impl == "reference":
+        return run_reference_arm(args, w, rank)
+
+    import lsgb300
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+    torch.cuda.set_device(local)
+    ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged)
+    nv = len(w["xyz"])
+    # L2 flush buffer (larger than the 129 MB L2), written between timed steps
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ls.step(1)
+    ls.reset_stats()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = 0.0
+    launched = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        before = ls.stats()["ms_total"]
+        launched += ls.step(1)
+        ms += ls.stats()["ms_total"] - before
+    barrier()
+    clocks.stop()
+    st = ls.stats()
+    updates = st["nb_vertex_updates"]
+    if dist is not None:
+        t = torch.tensor([ms, float(updates)], dtype=torch.float64)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        tsum = t.clone()
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        ms_job, updates_job = float(tmax[0]), float(tsum[1])
+    else:
+        ms_job, updates_job = ms, float(updates)
+    value = updates_job / (ms_job / 1000.0)
+    # our kernels launched inside the timed region (graph kernels included)
+    gpu_launches = int(st["kernel_launches"])
+
+    # end to end through the C ABI with host buffers: phi in (host) -> step -> phi out (host)
+    phi_h = ls.phi()
+    out_h = np.empty_like(phi_h)
+    e2e_steps = max(1, min(args.steps, 5))
+    before = ls.stats()["nb_vertex_updates"]
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ls.step_host(phi_h, out_h)
+        phi_h, out_h = out_h, phi_h
+    barrier()
+    e2e_sec = time.perf_counter() - t0
+    e2e_updates = ls.stats()["nb_vertex_updates"] - before
+    e2e_value = e2e_updates / e2e_sec
+
+    # roofline of the dominant kernel (FIM patch sweep): per-launch
+    # algorithmic slab bytes / per-launch device time, CUDA events on the
+    # library's stream around each sweep launch
+    ls.set_profile(True)
+    ls.reset_stats()
+    prof_steps = 2
+    ls.step(prof_steps)
+    ps = ls.stats()
+    ls.set_profile(False)
+    peak, peak_kind = load_peaks()
+    sweep_ms = ps["ms_sweep"] / max(ps["n_sweep"], 1)
+    bytes_per_launch = ps["sweep_slab_bytes"] / max(ps["n_sweep"], 1)
+    achieved = bytes_per_launch / (sweep_ms / 1000.0) / 1e9 if sweep_ms > 0 else 0.0
+    step_ms_prof = (ps["ms_sweep"] + ps["ms_check"] + ps["ms_schedule"] + ps["ms_seed"] + ps["ms_narrowband"]
+                    + ps["ms_update"])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profile_traffic(), "kernel": "k_fim<4,false> (FIM patch sweep)",
+                "peak_source": peak_kind,
+                "share_of_step": (ps["ms_sweep"] / step_ms_prof) if step_ms_prof > 0 else None,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": sweep_ms}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, sec, _ = oracle_rate(w, 2, 1, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "2 timed steps after 1 warm-up step of the full workload, FP32 oracle port (%.1f s)" % sec}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_job / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" + ("+f64flagged" if args.fp64_flagged else ""),
+            "data": "synthetic (seeded jittered cube, sphere-union SDF)",
+            "config": {"workload": w["label"], "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "fim_iters_per_step": st["fim_iters"] / args.steps,
+                       "patch_visits_per_step": st["patch_visits"] / args.steps,
+                       "check_visits_per_step": st["check_visits"] / args.steps,
+                       "nb_patches_per_step": st["nb_patches"] / args.steps,
+                       "flagged_fp64_solves": st["flagged_copies"]},
+            "clocks": clocks.summary(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * nv, "d2h_bytes_per_step": 4 * nv,
+                    "steps": e2e_steps},
+            "gpu_launches": gpu_launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,192 @@
+/*
+ * lsgb300.h -- C ABI of the GB300-native narrowband level-set time step.
+ *
+ * This is the drop-in boundary for the hot path of GPUTUM Level-Set
+ * (HongLi15/SCI-Solver_Level-Set): the narrowband time step on partitioned
+ * triangle / tetrahedral patches (seed -> fast-iterative-method redistance ->
+ * advection or mean-curvature update).  Plain C types only; the caller owns
+ * every array it passes and may free it after the call returns.  A handle is
+ * not thread-safe; each handle owns one CUDA stream on the current device.
+ * Every entry point returns an ls_status; ls_last_error() gives the reason.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   LevelSet::LevelSet / ~LevelSet            src/LevelSet.cu:4-33
+ *   LevelSet public parameters                src/LevelSet.h:49-60
+ *   LevelSet::initializeMesh                  src/LevelSet.cu:111-144
+ *   LevelSet::initializeVertices              src/LevelSet.cu:52-80
+ *   LevelSet::initializeAdvection             src/LevelSet.cu:82-109
+ *   meshFIM3d::Partition_METIS / GraphPartition_Square (partition input)
+ *                                             src/core3d/cuda/meshFIM3d.cu:269-421
+ *   meshFIM3d::InitPatches / InitPatches2 / GenerateBlockNeighbors
+ *                                             src/core3d/cuda/meshFIM3d.cu:423-570
+ *   LevelSet::solveLevelSet -> meshFIM3d::GenerateData (per-step loop)
+ *                                             src/LevelSet.cu:146-243,
+ *                                             src/core3d/cuda/meshFIM3d.cu:572-690
+ *   redistance3d::FindSeedPoint / ReInitTsign / GenerateData
+ *                                             src/core3d/cuda/redistance3d.cu:10-274
+ *   meshFIM3d::updateT_single_stage_d (advection)
+ *                                             src/core3d/cuda/meshFIM3d.cu:83-99
+ *   meshFIM3d::updateT_single_stage (curvature; host-only in the reference)
+ *                                             src/core3d/cuda/meshFIM3d.cu:103-267
+ *   LevelSet::getResultAtIteration / numIterations
+ *                                             src/LevelSet.cu:35-38
+ *   2D twins                                  src/core2d/cuda/meshFIM2d.cu:93-128,676-863,
+ *                                             src/core2d/cuda/redistance.cu:10-339
+ */
+#ifndef LSGB300_H
+#define LSGB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ls_status {
+  LS_OK = 0,
+  LS_BAD_INPUT = 1,         /* wrong sizes / indices / order of calls       */
+  LS_PATCH_TOO_LARGE = 2,   /* a patch exceeds 1024 element copies          */
+  LS_DEVICE_TIMEOUT = 3,    /* the FIM loop exceeded max_fim_iters          */
+  LS_CUDA_ERROR = 4,        /* a CUDA call failed                           */
+  LS_NOT_READY = 5,         /* ls_setup has not run                         */
+  LS_NO_MEMORY = 6          /* device or host allocation failed             */
+} ls_status;
+
+/* Update applied after the redistance of each step. */
+enum { LS_UPDATE_ADVECT = 0, LS_UPDATE_CURVATURE = 1, LS_UPDATE_NONE = 2 };
+
+/* Flags. */
+enum {
+  /* Reproduce the reference's arithmetic choices: absolute SMALLNUM in the
+   * tet solver and convergence test, patch-constant velocity (3D), the 2D
+   * velocity replaced by (phi0, phi1)/|grad phi|, and the reference host
+   * curvature formula (sigma = (1,0,1) gate, no mass-lumping factor). */
+  LS_REF_COMPAT = 1u << 0,
+  /* Precision form: a tet local solve whose quadratic discriminant cancels
+   * in FP32 (|q^2 - 4pr| <= fp64_threshold * (q^2 + |4pr|)) is repeated in
+   * FP64; all other arithmetic stays FP32. */
+  LS_FP64_FLAGGED = 1u << 1,
+  /* Record per-kernel CUDA-event timings (ls_get_stats). */
+  LS_PROFILE = 1u << 2,
+  /* Do not use CUDA graphs for the FIM iteration chunks. */
+  LS_NO_GRAPH = 1u << 3
+};
+
+typedef struct ls_params {
+  /* reference LevelSet fields (src/LevelSet.h:51-58, defaults LevelSet.cu:4-22) */
+  int num_steps;          /* numSteps_         (10)   */
+  double time_step;       /* timeStep_         (1.0)  */
+  int inside_iterations;  /* insideIterations_ (1)    */
+  int block_size;         /* blockSize_        (16)   structured partition block side */
+  int side_lengths;       /* sideLengths_      (1)    structured partition side       */
+  double bandwidth;       /* bandwidth_        (16.0) */
+  int metis_size;         /* metisSize_        (16)   target vertices per graph patch */
+  int partition_type;     /* partitionType_    (0)    0 graph, 1 structured blocks    */
+  int verbose;            /* verbose_          (0)    */
+  /* extensions */
+  int update_kind;        /* LS_UPDATE_*       (ADVECT) */
+  double curv_coeff;      /* curvature coefficient (1.0) */
+  unsigned flags;         /* LS_* flags        (0)    */
+  int fim_sweeps;         /* sweeps per patch visit (0 -> 5 in 3D, 10 in 2D) */
+  int max_fim_iters;      /* FIM iterations per step before LS_DEVICE_TIMEOUT (0 -> 100000) */
+  double smallnum;        /* 0 -> 1e-5 */
+  double largenum;        /* 0 -> 1e9  */
+  double length_scale;    /* FIM length unit when not LS_REF_COMPAT (0 -> mean edge length) */
+  double fp64_threshold;  /* LS_FP64_FLAGGED: discriminant cancellation threshold tau (0 -> 2^-18) */
+  int graph_chunk;        /* FIM iterations per graph launch / host check (0 -> 4) */
+} ls_params;
+
+typedef struct ls_stats {
+  int steps_run;
+  long long fim_iters;          /* FIM outer iterations, all steps          */
+  long long patch_visits;       /* patch sweeps (NITER sweeps each)         */
+  long long check_visits;       /* neighbour checks (one sweep each)        */
+  long long nb_vertex_updates;  /* sum over steps of #{v : |phi(v)| <= w}   */
+  long long nb_patch_vertices;  /* sum over steps of sum_{p in NB} nv_p     */
+  long long nb_patches;         /* sum over steps of |NB|                   */
+  long long flagged_copies;     /* local solves repeated in FP64 (precision form) */
+  double ms_total;              /* device time of ls_step / ls_solve calls  */
+  /* LS_PROFILE only: per-kernel device time (ms) and launches */
+  double ms_sweep, ms_check, ms_schedule, ms_seed, ms_narrowband, ms_update;
+  long long n_sweep, n_check, n_schedule, n_seed, n_narrowband, n_update;
+  long long sweep_slab_bytes;   /* algorithmic bytes read+written by sweeps */
+  long long kernel_launches;    /* kernels launched (graph kernels included) */
+} ls_stats;
+
+typedef struct ls_handle ls_handle;
+
+ls_status ls_default_params(ls_params* p);
+/* LevelSet(bool isTriMesh, ...): src/LevelSet.cu:4-22 */
+ls_status ls_create(ls_handle** h, int is_tri);
+/* ~LevelSet: src/LevelSet.cu:24-33 */
+ls_status ls_destroy(ls_handle* h);
+ls_status ls_set_params(ls_handle* h, const ls_params* p);
+ls_status ls_get_params(ls_handle* h, ls_params* p);
+/* initializeMesh: xyz nv*3 floats, elems ne*(3|4) ints (0-based). */
+ls_status ls_set_mesh(ls_handle* h, const float* xyz, int nv, const int* elems, int ne);
+/* Partition input (replaces Partition_METIS / GraphPartition_Square):
+ * npart nv ints in [0, nparts).  Optional; ls_setup partitions otherwise. */
+ls_status ls_set_partition(ls_handle* h, const int* npart, int nparts);
+/* initializeVertices: phi nv floats in the caller's vertex order. */
+ls_status ls_set_phi(ls_handle* h, const float* phi);
+/* initializeAdvection: vel ne*3 floats, one vector per element. */
+ls_status ls_set_velocity(ls_handle* h, const float* vel);
+/* Host part of the preprocessing only (partition if not given, default phi
+ * and velocity, patch layout); no device work.  ls_setup calls it. */
+ls_status ls_prepare(ls_handle* h);
+/* Preprocessing of GenerateData (meshFIM3d.cu:592-629): partition (if not
+ * given), patch layout, device upload.  Allocates all device memory. */
+ls_status ls_setup(ls_handle* h);
+/* GenerateData's time loop (meshFIM3d.cu:639-678): nsteps steps from the
+ * current phi.  history (optional): (nsteps+1)*nv floats, row 0 = phi at
+ * entry, row s = phi after step s (caller's vertex order), copied to the host
+ * after every step as the reference does.  Stops early when the narrowband
+ * is empty (meshFIM3d.cu:655-659); *steps_done reports the steps run. */
+ls_status ls_solve(ls_handle* h, int nsteps, float* history, int* steps_done);
+/* Device-resident steps: no host copies of phi. */
+ls_status ls_step(ls_handle* h, int nsteps, int* steps_done);
+/* End-to-end step through host buffers: phi_in (nv floats, host) is copied
+ * to the device, one step runs, phi_out (host) receives the result. */
+ls_status ls_step_host(ls_handle* h, const float* phi_in, float* phi_out);
+/* Current phi in the caller's vertex order. */
+ls_status ls_get_phi(ls_handle* h, float* phi);
+ls_status ls_get_stats(ls_handle* h, ls_stats* s);
+ls_status ls_reset_stats(ls_handle* h);
+/* Turn per-kernel CUDA-event timing on or off for the following steps
+ * (kernels are then launched one by one instead of from the graph). */
+ls_status ls_set_profile(ls_handle* h, int on);
+/* Narrowband of the last step: one byte per patch. */
+ls_status ls_get_narrowband(ls_handle* h, unsigned char* flags);
+/* info[0..9] = nparts, full, lep, lvp, lgp, lim, nadj, nv, ne, dim */
+ls_status ls_get_layout_info(ls_handle* h, long long* info);
+/* Reference-format layout arrays (LS_REF_* below) for bit-exact checks. */
+ls_status ls_get_layout(ls_handle* h, int which, void* dst);
+const char* ls_last_error(ls_handle* h);
+const char* ls_version(void);
+
+/* Layout array selectors for ls_get_layout (meshFIM3d members). */
+enum {
+  LS_REF_ELE_PERMUTE = 0,          /* int[full]           ele_permute          */
+  LS_REF_ELE_OFFSETS = 1,          /* int[nparts+1]       m_ele_offsets_d      */
+  LS_REF_VERT_PERMUTE = 2,         /* int[nv]             m_vert_permute_d     */
+  LS_REF_VERT_OFFSETS = 3,         /* int[nparts+1]       m_vert_offsets_d     */
+  LS_REF_ELE_AFTER_PERMUTE = 4,    /* int[(d+1)*full]     m_ele_after_permute_d*/
+  LS_REF_MEM_LOCATIONS = 5,        /* int[(d+1)*full]     m_mem_locations      */
+  LS_REF_MEM_LOCATION_OFFSETS = 6, /* int[nv+1]           m_mem_location_offsets */
+  LS_REF_BLOCK_XADJ = 7,           /* int[nparts+1]       m_block_xadj_d       */
+  LS_REF_BLOCK_ADJNCY = 8,         /* int[nadj]           m_block_adjncy_d     */
+  LS_REF_LOCAL_COORDS = 9,         /* float[6|3 * full]   m_ele_local_coords_d */
+  LS_REF_VERT_IPERMUTE = 10        /* int[nv]             vert_ipermute        */
+};
+
+/* Partitioners.  Structured blocks: GraphPartition_Square semantics
+ * (meshFIM3d.cu:316-326, meshFIM2d.cu:346-353) on an x-fastest lattice of
+ * side nside (3D: nside^3 vertices, 2D: nside^2), block side block. */
+ls_status ls_partition_structured(int dim, int nside, int block, int nv, int* npart, int* nparts);
+/* Graph partition stand-in for METIS_PartGraphKway (meshFIM3d.cu:354-421):
+ * recursive coordinate bisection into ceil(nv / target) parts (3D) or
+ * max(2, nv / target) parts (2D, meshFIM2d.cu:380-382). */
+ls_status ls_partition_rcb(int dim, const float* xyz, int nv, int target, int* npart, int* nparts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,70 @@
+"""Build oracle/_ref/: parts of the reference compiled from its own sources.
+
+Recipe (test infrastructure only).  Compiles, with nvcc and the shim headers
+in oracle/ref_shim/, directly from the reference tree (read-only):
+  libref_tet.so  localSolverTet1Levelset  (src/core3d/include/redistance_kernels3d.h)
+  libref_tri.so  localSolverTri, localSolverTet1 (src/core2d/include/redistance_kernels.h)
+  libref_k20.so  meshFIM3d::updateT_single_stage from src/core3d/cuda/meshFIM3d.cu
+                 (+ src/core3d/cuda/redistance3d.cu, which it links against)
+Nothing is copied out of the reference tree; outputs go only to oracle/_ref/.
+
+Usage: python oracle/build_ref.py [REFERENCE_ROOT]   (default /root/reference)
+Constants the reference takes from its missing dependency: LARGENUM = 1e9,
+SMALLNUM = 1e-5 (the value src/core2d/include/redistance.h:17-19 uses).
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+SHIM = os.path.join(HERE, "ref_shim")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    for c in ("/usr/local/cuda/bin/nvcc", "nvcc"):
+        if os.path.sep not in c or os.path.exists(c):
+            return c
+    return "nvcc"
+
+
+def run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def build(ref_root="/root/reference"):
+    src = os.path.join(ref_root, "src")
+    if not os.path.isdir(src):
+        return False
+    os.makedirs(OUT, exist_ok=True)
+    base = [nvcc(), "-std=c++17", "-O2", "-Xcompiler", "-fPIC,-ffp-contract=off", "-w"] + ARCH + [
+        "-I" + SHIM, "-include", os.path.join(SHIM, "prelude.h"), "-DSMALLNUM=1e-5"]
+    inc3 = ["-I" + os.path.join(src, "core3d", "include")]
+    inc2 = ["-I" + os.path.join(src, "core2d", "include")]
+    jobs = [
+        (base + inc3 + ["-c", os.path.join(HERE, "ref_harness_tet.cu"), "-o", os.path.join(OUT, "tet.o")]),
+        (base + inc2 + ["-c", os.path.join(HERE, "ref_harness_tri.cu"), "-o", os.path.join(OUT, "tri.o")]),
+        (base + inc3 + ["-DLSREF_HOST_ONLY", "-c", os.path.join(src, "core3d", "cuda", "meshFIM3d.cu"),
+                        "-o", os.path.join(OUT, "meshFIM3d.o")]),
+        (base + inc3 + ["-DLSREF_HOST_ONLY", "-c", os.path.join(src, "core3d", "cuda", "redistance3d.cu"),
+                        "-o", os.path.join(OUT, "redistance3d.o")]),
+        (base + inc3 + ["-DLSREF_HOST_ONLY", "-c", os.path.join(HERE, "ref_harness_k20.cu"),
+                        "-o", os.path.join(OUT, "k20.o")]),
+    ]
+    with ThreadPoolExecutor(max_workers=5) as ex:
+        list(ex.map(run, jobs))
+    link = [nvcc(), "-shared"] + ARCH
+    run(link + [os.path.join(OUT, "tet.o"), "-o", os.path.join(OUT, "libref_tet.so")])
+    run(link + [os.path.join(OUT, "tri.o"), "-o", os.path.join(OUT, "libref_tri.so")])
+    run(link + [os.path.join(OUT, n) for n in ("k20.o", "meshFIM3d.o", "redistance3d.o")] +
+        ["-o", os.path.join(OUT, "libref_k20.so")])
+    return True
+
+
+if __name__ == "__main__":
+    ok = build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    print("built" if ok else "reference tree not found; nothing built")

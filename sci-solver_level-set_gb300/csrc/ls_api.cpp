@@ -1,0 +1,382 @@
+// ls_api.cpp -- C ABI (include/lsgb300.h) over the layout builder and the
+// device solver.  Mirrors the call sequence of LevelSet (src/LevelSet.cu):
+// create -> mesh -> phi / velocity -> solve -> results, with status codes in
+// place of the reference's exit(0) on bad input.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/lsgb300.h"
+#include "ls_layout.h"
+#include "ls_solver.h"
+
+struct ls_handle {
+  int is_tri = 0;
+  ls_params prm;
+  std::vector<float> xyz;
+  std::vector<int> elems;
+  int nv = 0, ne = 0;
+  std::vector<int> npart;
+  int nparts = 0;
+  std::vector<float> phi;
+  std::vector<float> vel;
+  bool have_phi = false, have_vel = false;
+  std::unique_ptr<lsgb::Layout> layout;
+  std::unique_ptr<lsgb::Solver> solver;
+  std::string err;
+};
+
+namespace {
+ls_status fail(ls_handle* h, ls_status s, const std::string& msg) {
+  if (h) h->err = msg;
+  return s;
+}
+
+ls_status solver_status(ls_handle* h, const std::string& msg) {
+  if (msg.empty()) return LS_OK;
+  h->err = msg;
+  switch (h->solver ? h->solver->status_code() : 4) {
+    case 2: return LS_PATCH_TOO_LARGE;
+    case 3: return LS_DEVICE_TIMEOUT;
+    default: return LS_CUDA_ERROR;
+  }
+}
+
+// Recursive coordinate bisection: split the longest extent at the median
+// until each part holds at most `target` vertices.
+void rcb(const float* xyz, std::vector<int>& idx, int lo, int hi, int nparts, int first, int* npart) {
+  if (nparts <= 1 || hi - lo <= 1) {
+    for (int i = lo; i < hi; ++i) npart[idx[i]] = first;
+    return;
+  }
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = lo; i < hi; ++i)
+    for (int j = 0; j < 3; ++j) {
+      mn[j] = std::min(mn[j], xyz[(size_t)idx[i] * 3 + j]);
+      mx[j] = std::max(mx[j], xyz[(size_t)idx[i] * 3 + j]);
+    }
+  int ax = 0;
+  for (int j = 1; j < 3; ++j)
+    if (mx[j] - mn[j] > mx[ax] - mn[ax]) ax = j;
+  const int left = nparts / 2;
+  const int mid = lo + (int)((long long)(hi - lo) * left / nparts);
+  std::nth_element(idx.begin() + lo, idx.begin() + mid, idx.begin() + hi, [&](int a, int b) {
+    float xa = xyz[(size_t)a * 3 + ax], xb = xyz[(size_t)b * 3 + ax];
+    return xa < xb || (xa == xb && a < b);
+  });
+  rcb(xyz, idx, lo, mid, left, first, npart);
+  rcb(xyz, idx, mid, hi, nparts - left, first + left, npart);
+}
+}  // namespace
+
+extern "C" {
+
+const char* ls_version(void) { return "lsgb300 1.0 (sm_103a)"; }
+
+ls_status ls_default_params(ls_params* p) {
+  if (!p) return LS_BAD_INPUT;
+  std::memset(p, 0, sizeof(*p));
+  p->num_steps = 10;
+  p->time_step = 1.0;
+  p->inside_iterations = 1;
+  p->block_size = 16;
+  p->side_lengths = 1;
+  p->bandwidth = 16.0;
+  p->metis_size = 16;
+  p->partition_type = 0;
+  p->verbose = 0;
+  p->update_kind = LS_UPDATE_ADVECT;
+  p->curv_coeff = 1.0;
+  p->flags = 0;
+  p->fim_sweeps = 0;
+  p->max_fim_iters = 100000;
+  p->smallnum = 1e-5;
+  p->largenum = 1e9;
+  p->length_scale = 0.0;
+  p->fp64_threshold = 3.814697265625e-06;
+  p->graph_chunk = 4;
+  return LS_OK;
+}
+
+ls_status ls_create(ls_handle** h, int is_tri) {
+  if (!h) return LS_BAD_INPUT;
+  ls_handle* x = new (std::nothrow) ls_handle();
+  if (!x) return LS_NO_MEMORY;
+  x->is_tri = is_tri ? 1 : 0;
+  ls_default_params(&x->prm);
+  *h = x;
+  return LS_OK;
+}
+
+ls_status ls_destroy(ls_handle* h) {
+  delete h;
+  return LS_OK;
+}
+
+const char* ls_last_error(ls_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+ls_status ls_set_params(ls_handle* h, const ls_params* p) {
+  if (!h || !p) return LS_BAD_INPUT;
+  if (p->inside_iterations < 0 || p->bandwidth < 0 || p->update_kind < 0 || p->update_kind > 2)
+    return fail(h, LS_BAD_INPUT, "invalid parameter");
+  h->prm = *p;
+  h->solver.reset();  // parameters are baked into the device setup
+  return LS_OK;
+}
+
+ls_status ls_get_params(ls_handle* h, ls_params* p) {
+  if (!h || !p) return LS_BAD_INPUT;
+  *p = h->prm;
+  return LS_OK;
+}
+
+ls_status ls_set_mesh(ls_handle* h, const float* xyz, int nv, const int* elems, int ne) {
+  if (!h) return LS_BAD_INPUT;
+  if (!xyz || !elems || nv <= 0 || ne <= 0) return fail(h, LS_BAD_INPUT, "empty mesh");
+  const int d1 = h->is_tri ? 3 : 4;
+  for (long long i = 0; i < (long long)ne * d1; ++i)
+    if (elems[i] < 0 || elems[i] >= nv) return fail(h, LS_BAD_INPUT, "element vertex index out of range");
+  h->xyz.assign(xyz, xyz + (size_t)nv * 3);
+  h->elems.assign(elems, elems + (size_t)ne * d1);
+  h->nv = nv;
+  h->ne = ne;
+  h->npart.clear();
+  h->nparts = 0;
+  h->have_phi = h->have_vel = false;
+  h->layout.reset();
+  h->solver.reset();
+  return LS_OK;
+}
+
+ls_status ls_set_partition(ls_handle* h, const int* npart, int nparts) {
+  if (!h) return LS_BAD_INPUT;
+  if (h->nv == 0) return fail(h, LS_BAD_INPUT, "set the mesh first");
+  if (!npart || nparts <= 0) return fail(h, LS_BAD_INPUT, "empty partition");
+  for (int v = 0; v < h->nv; ++v)
+    if (npart[v] < 0 || npart[v] >= nparts) return fail(h, LS_BAD_INPUT, "partition label out of range");
+  h->npart.assign(npart, npart + h->nv);
+  h->nparts = nparts;
+  h->layout.reset();
+  h->solver.reset();
+  return LS_OK;
+}
+
+ls_status ls_set_phi(ls_handle* h, const float* phi) {
+  if (!h) return LS_BAD_INPUT;
+  if (h->nv == 0) return fail(h, LS_BAD_INPUT, "You must initialize the mesh first!");
+  if (!phi) return fail(h, LS_BAD_INPUT, "null phi");
+  h->phi.assign(phi, phi + h->nv);
+  h->have_phi = true;
+  if (h->solver) return solver_status(h, h->solver->set_phi(phi));
+  return LS_OK;
+}
+
+ls_status ls_set_velocity(ls_handle* h, const float* vel) {
+  if (!h) return LS_BAD_INPUT;
+  if (h->nv == 0) return fail(h, LS_BAD_INPUT, "You must initialize the mesh first!");
+  if (!vel) return fail(h, LS_BAD_INPUT, "null velocity");
+  h->vel.assign(vel, vel + (size_t)h->ne * 3);
+  h->have_vel = true;
+  h->solver.reset();
+  return LS_OK;
+}
+
+ls_status ls_partition_structured(int dim, int nside, int block, int nv, int* npart, int* nparts) {
+  if ((dim != 2 && dim != 3) || nside <= 0 || block <= 0 || !npart || !nparts) return LS_BAD_INPUT;
+  const long long expect = dim == 3 ? (long long)nside * nside * nside : (long long)nside * nside;
+  if (expect != nv) return LS_BAD_INPUT;
+  const int nb = (nside + block - 1) / block;
+  if (dim == 3) {
+    for (int k = 0; k < nside; ++k)
+      for (int i = 0; i < nside; ++i)
+        for (int j = 0; j < nside; ++j)
+          npart[(size_t)k * nside * nside + (size_t)i * nside + j] = (k / block) * nb * nb + (i / block) * nb + (j / block);
+    *nparts = nb * nb * nb;
+  } else {
+    for (int i = 0; i < nside; ++i)
+      for (int j = 0; j < nside; ++j) npart[(size_t)i * nside + j] = (i / block) * nb + (j / block);
+    *nparts = nb * nb;
+  }
+  return LS_OK;
+}
+
+ls_status ls_partition_rcb(int dim, const float* xyz, int nv, int target, int* npart, int* nparts) {
+  if ((dim != 2 && dim != 3) || !xyz || nv <= 0 || target <= 0 || !npart || !nparts) return LS_BAD_INPUT;
+  int np = dim == 3 ? (int)std::ceil((double)nv / target) : std::max(2, nv / target);
+  np = std::max(1, std::min(np, nv));
+  std::vector<int> idx(nv);
+  std::iota(idx.begin(), idx.end(), 0);
+  rcb(xyz, idx, 0, nv, np, 0, npart);
+  *nparts = np;
+  return LS_OK;
+}
+
+ls_status ls_prepare(ls_handle* h) {
+  if (!h) return LS_BAD_INPUT;
+  if (h->nv == 0) return fail(h, LS_BAD_INPUT, "You must initialize the mesh first!");
+  const int dim = h->is_tri ? 2 : 3;
+  if (h->npart.empty()) {
+    h->npart.resize(h->nv);
+    ls_status s;
+    if (h->prm.partition_type == 1)
+      s = ls_partition_structured(dim, h->prm.side_lengths, h->prm.block_size, h->nv, h->npart.data(), &h->nparts);
+    else
+      s = ls_partition_rcb(dim, h->xyz.data(), h->nv, h->prm.metis_size, h->npart.data(), &h->nparts);
+    if (s != LS_OK) {
+      h->npart.clear();
+      return fail(h, s, "partitioning failed (structured partition needs side_lengths^dim vertices)");
+    }
+  }
+  if (!h->have_phi) {
+    // LevelSet.cu:194-199 / 228-233: phi0 = x - midX
+    float mn = INFINITY, mx = -INFINITY;
+    for (int v = 0; v < h->nv; ++v) {
+      mn = std::min(mn, h->xyz[(size_t)v * 3]);
+      mx = std::max(mx, h->xyz[(size_t)v * 3]);
+    }
+    const double mid = ((double)mn + (double)mx) / 2.0;
+    h->phi.resize(h->nv);
+    for (int v = 0; v < h->nv; ++v) h->phi[v] = (float)(h->xyz[(size_t)v * 3] - mid);
+    h->have_phi = true;
+  }
+  if (!h->have_vel) {
+    // LevelSet.cu:187-192 / 221-226: 3D (rangeX/100, 0, 0), 2D zero
+    float mn = INFINITY, mx = -INFINITY;
+    for (int v = 0; v < h->nv; ++v) {
+      mn = std::min(mn, h->xyz[(size_t)v * 3]);
+      mx = std::max(mx, h->xyz[(size_t)v * 3]);
+    }
+    const float vx = h->is_tri ? 0.f : (float)(((double)mx - mn) / 100.0);
+    h->vel.assign((size_t)h->ne * 3, 0.f);
+    for (int e = 0; e < h->ne; ++e) h->vel[(size_t)e * 3] = vx;
+    h->have_vel = true;
+  }
+  if (!h->layout) {
+    auto L = std::make_unique<lsgb::Layout>();
+    std::string r = lsgb::build_layout(dim, h->nv, h->xyz.data(), h->ne, h->elems.data(), h->npart.data(),
+                                       h->nparts, *L);
+    if (!r.empty()) return fail(h, LS_BAD_INPUT, r);
+    if (L->lep > 1024) return fail(h, LS_PATCH_TOO_LARGE, "Error: largest_ele_part > 1024");
+    h->layout = std::move(L);
+  }
+  return LS_OK;
+}
+
+ls_status ls_setup(ls_handle* h) {
+  ls_status ps = ls_prepare(h);
+  if (ps != LS_OK) return ps;
+  lsgb::SolverConfig cfg;
+  const ls_params& p = h->prm;
+  cfg.update_kind = p.update_kind;
+  cfg.ref_compat = (p.flags & LS_REF_COMPAT) ? 1 : 0;
+  cfg.fp64_flagged = (p.flags & LS_FP64_FLAGGED) ? 1 : 0;
+  cfg.profile = (p.flags & LS_PROFILE) ? 1 : 0;
+  cfg.use_graph = (p.flags & LS_NO_GRAPH) ? 0 : 1;
+  cfg.niter = p.fim_sweeps;
+  cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
+  cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;
+  cfg.graph_chunk = p.graph_chunk > 0 ? p.graph_chunk : 4;
+  cfg.dt = p.time_step;
+  cfg.bandwidth = p.bandwidth;
+  cfg.curv_coeff = p.curv_coeff;
+  cfg.smallnum = p.smallnum > 0 ? p.smallnum : 1e-5;
+  cfg.largenum = p.largenum > 0 ? p.largenum : 1e9;
+  cfg.length_scale = p.length_scale;
+  if (p.fp64_threshold > 0) cfg.fp64_tau = p.fp64_threshold;
+  h->solver = std::make_unique<lsgb::Solver>();
+  std::string r = h->solver->init(*h->layout, cfg, h->vel.data());
+  if (!r.empty()) {
+    ls_status s = solver_status(h, r);
+    h->solver.reset();
+    return s;
+  }
+  return solver_status(h, h->solver->set_phi(h->phi.data()));
+}
+
+ls_status ls_solve(ls_handle* h, int nsteps, float* history, int* steps_done) {
+  if (!h) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  if (nsteps < 0) return fail(h, LS_BAD_INPUT, "negative step count");
+  return solver_status(h, h->solver->run(nsteps, history, steps_done));
+}
+
+ls_status ls_step(ls_handle* h, int nsteps, int* steps_done) { return ls_solve(h, nsteps, nullptr, steps_done); }
+
+ls_status ls_step_host(ls_handle* h, const float* phi_in, float* phi_out) {
+  if (!h) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  if (!phi_in || !phi_out) return fail(h, LS_BAD_INPUT, "null buffer");
+  return solver_status(h, h->solver->step_host(phi_in, phi_out));
+}
+
+ls_status ls_get_phi(ls_handle* h, float* phi) {
+  if (!h || !phi) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  return solver_status(h, h->solver->get_phi(phi));
+}
+
+ls_status ls_get_stats(ls_handle* h, ls_stats* s) {
+  if (!h || !s) return LS_BAD_INPUT;
+  std::memset(s, 0, sizeof(*s));
+  if (!h->solver) return LS_OK;
+  lsgb::SolverStats t;
+  h->solver->stats(t);
+  s->steps_run = (int)t.steps_run;
+  s->fim_iters = t.fim_iters;
+  s->patch_visits = t.patch_visits;
+  s->check_visits = t.check_visits;
+  s->nb_vertex_updates = t.nb_vertex_updates;
+  s->nb_patch_vertices = t.nb_patch_vertices;
+  s->nb_patches = t.nb_patches;
+  s->flagged_copies = t.flagged_copies;
+  s->ms_total = t.ms_total;
+  s->ms_sweep = t.ms_sweep; s->ms_check = t.ms_check; s->ms_schedule = t.ms_schedule;
+  s->ms_seed = t.ms_seed; s->ms_narrowband = t.ms_narrowband; s->ms_update = t.ms_update;
+  s->n_sweep = t.n_sweep; s->n_check = t.n_check; s->n_schedule = t.n_schedule;
+  s->n_seed = t.n_seed; s->n_narrowband = t.n_narrowband; s->n_update = t.n_update;
+  s->sweep_slab_bytes = t.sweep_slab_bytes;
+  s->kernel_launches = t.kernel_launches;
+  return LS_OK;
+}
+
+ls_status ls_set_profile(ls_handle* h, int on) {
+  if (!h) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  h->solver->set_profile(on != 0);
+  return LS_OK;
+}
+
+ls_status ls_reset_stats(ls_handle* h) {
+  if (!h) return LS_BAD_INPUT;
+  if (h->solver) h->solver->reset_stats();
+  return LS_OK;
+}
+
+ls_status ls_get_narrowband(ls_handle* h, unsigned char* flags) {
+  if (!h || !flags) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  return solver_status(h, h->solver->narrowband(flags));
+}
+
+ls_status ls_get_layout_info(ls_handle* h, long long* info) {
+  if (!h || !info) return LS_BAD_INPUT;
+  if (!h->layout) return fail(h, LS_NOT_READY, "call ls_setup first");
+  const lsgb::Layout& L = *h->layout;
+  info[0] = L.nparts; info[1] = L.full; info[2] = L.lep; info[3] = L.lvp; info[4] = L.lgp;
+  info[5] = L.lim; info[6] = lsgb::ref_array_size(L, lsgb::REF_BLOCK_ADJNCY); info[7] = L.nv;
+  info[8] = L.ne; info[9] = L.dim;
+  return LS_OK;
+}
+
+ls_status ls_get_layout(ls_handle* h, int which, void* dst) {
+  if (!h || !dst) return LS_BAD_INPUT;
+  if (!h->layout) return fail(h, LS_NOT_READY, "call ls_setup first");
+  if (!lsgb::ref_array_copy(*h->layout, which, dst)) return fail(h, LS_BAD_INPUT, "unknown layout array");
+  return LS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,410 @@
+// ls_solver.cu -- host orchestration of the device time step.
+//
+// The reference drives its FIM loop from the host with two synchronous
+// device->host copies and a host list update per iteration
+// (src/core3d/cuda/redistance3d.cu:85-224).  Here the lists, labels and
+// convergence flags stay on the device; the host only launches a fixed
+// chunk of FIM iterations (captured once as a CUDA graph) and reads one
+// counter per chunk to learn whether the active list has drained.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ls_solver.h"
+
+namespace lsgb {
+
+namespace {
+template <typename T>
+cudaError_t dalloc(std::vector<void*>& list, T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
+  if (e == cudaSuccess) list.push_back(*p);
+  return e;
+}
+template <typename T>
+cudaError_t upload(std::vector<void*>& list, const T** p, const std::vector<T>& v, cudaStream_t st) {
+  T* d = nullptr;
+  cudaError_t e = dalloc(list, &d, v.size());
+  if (e != cudaSuccess) return e;
+  if (!v.empty()) e = cudaMemcpyAsync(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+  *p = d;
+  return e;
+}
+
+}  // namespace
+
+Solver::~Solver() {
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (graph_) cudaGraphDestroy(graph_);
+  for (void* p : allocs_) cudaFree(p);
+  if (h_counts_) cudaFreeHost(h_counts_);
+  if (h_stats_) cudaFreeHost(h_stats_);
+  if (h_stage_) cudaFreeHost(h_stage_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+std::string Solver::check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return "";
+  status_ = 4;
+  return std::string(what) + ": " + cudaGetErrorString(e);
+}
+
+#define LS_TRY(expr, what)                         \
+  do {                                             \
+    std::string _m = check((expr), (what));        \
+    if (!_m.empty()) return _m;                    \
+  } while (0)
+
+std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* vel) {
+  lay_ = &L;
+  cfg_ = cfg;
+  if (L.lep > 1024) { status_ = 2; return "a patch has more than 1024 element copies"; }
+  LS_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  LS_TRY(cudaEventCreate(&ev0_), "event");
+  LS_TRY(cudaEventCreate(&ev1_), "event");
+  const int nv = L.nv, np = L.nparts;
+  const long long full = L.full;
+  const int d1 = L.dim + 1;
+
+  // per-copy arrays
+  std::vector<ushort4> conn(full);
+  for (long long c = 0; c < full; ++c)
+    conn[c] = make_ushort4(L.conn_local[c * 4], L.conn_local[c * 4 + 1], L.conn_local[c * 4 + 2],
+                           L.conn_local[c * 4 + 3]);
+  const int nc = L.dim == 3 ? 6 : 3;
+  std::vector<float> lc((size_t)nc * full), sig((size_t)3 * full, 0.f);
+  // FIM frame: without the reference's semantics, lengths are divided by
+  // the mesh scale (mean edge length unless given) so that the local
+  // solver's polynomial terms are O(1) in FP32 whatever the caller's units.
+  const bool ref = cfg.ref_compat != 0;
+  const double scale = ref ? 1.0 : (cfg.length_scale > 0 ? cfg.length_scale : L.mean_edge);
+  for (long long c = 0; c < full; ++c) {
+    const int e = L.ele_permute[c];
+    if (L.dim == 3) {
+      float P[4][3], Lc[6];
+      for (int k = 0; k < 4; ++k)
+        for (int j = 0; j < 3; ++j) P[k][j] = L.xyz_p[(size_t)j * nv + L.conn[c * 4 + k]];
+      tet_local_coords(P, Lc);
+      for (int i = 0; i < 6; ++i) lc[i * full + c] = ref ? Lc[i] : (float)((double)Lc[i] / scale);
+      if (vel)
+        for (int j = 0; j < 3; ++j) sig[j * full + c] = vel[(size_t)e * 3 + j];
+    } else {
+      double P[3][3], Lc[3], sg[2], vv[3] = {0, 0, 0};
+      for (int k = 0; k < 3; ++k)
+        for (int j = 0; j < 3; ++j) P[k][j] = L.xyz_p[(size_t)j * nv + L.conn[c * 3 + k]];
+      if (vel)
+        for (int j = 0; j < 3; ++j) vv[j] = vel[(size_t)e * 3 + j];
+      tri_local_coords(P, vv, Lc, sg);
+      for (int i = 0; i < 3; ++i) lc[i * full + c] = (float)(ref ? Lc[i] : Lc[i] / scale);
+      sig[c] = (float)sg[0];
+      sig[full + c] = (float)sg[1];
+    }
+  }
+  // per-patch algorithmic bytes of one FIM visit: owned DT read + DT_out
+  // write + seed flags, ghost ids + ghost DT, connectivity (8 B) and local
+  // coordinates (4 B each) per copy, 3 patch offsets pairs
+  std::vector<int> pbytes(np);
+  for (int p = 0; p < np; ++p) {
+    const long long nvp = L.vert_offsets[p + 1] - L.vert_offsets[p];
+    const long long ngp = L.ghost_offsets[p + 1] - L.ghost_offsets[p];
+    const long long nep = L.ele_offsets[p + 1] - L.ele_offsets[p];
+    pbytes[p] = (int)(nvp * (4 + 4 + 1) + ngp * (4 + 4) + nep * (8 + 4 * nc) + 24);
+  }
+  std::vector<int> ipermute(L.vert_ipermute);
+
+  m_.dim = L.dim; m_.nv = nv; m_.nparts = np; m_.full = full;
+  std::vector<void*>& A = allocs_;
+  LS_TRY(upload(A, &m_.vert_off, L.vert_offsets, stream_), "upload");
+  LS_TRY(upload(A, &m_.ele_off, L.ele_offsets, stream_), "upload");
+  LS_TRY(upload(A, &m_.ghost_off, L.ghost_offsets, stream_), "upload");
+  LS_TRY(upload(A, &m_.ghost_ids, L.ghost_ids, stream_), "upload");
+  LS_TRY(upload(A, &m_.conn, conn, stream_), "upload");
+  LS_TRY(upload(A, &m_.lc, lc, stream_), "upload");
+  LS_TRY(upload(A, &m_.sig, sig, stream_), "upload");
+  LS_TRY(upload(A, &m_.vslot_off, L.vslot_off, stream_), "upload");
+  LS_TRY(upload(A, &m_.vslot, L.vslot, stream_), "upload");
+  LS_TRY(upload(A, &m_.padj_off, L.padj_off, stream_), "upload");
+  LS_TRY(upload(A, &m_.padj, L.padj, stream_), "upload");
+  LS_TRY(upload(A, &m_.xyz, L.xyz_p, stream_), "upload");
+  LS_TRY(upload(A, &m_.ipermute, ipermute, stream_), "upload");
+  LS_TRY(upload(A, &m_.patch_bytes, pbytes, stream_), "upload");
+  // step state
+  LS_TRY(dalloc(A, &s_.phi, nv), "alloc");
+  LS_TRY(dalloc(A, &s_.phi_out, nv), "alloc");
+  LS_TRY(dalloc(A, &s_.DT, nv), "alloc");
+  LS_TRY(dalloc(A, &s_.DT_out, nv), "alloc");
+  LS_TRY(dalloc(A, &s_.seed, nv), "alloc");
+  LS_TRY(dalloc(A, &s_.sign, nv), "alloc");
+  LS_TRY(dalloc(A, &s_.blabel, np), "alloc");
+  LS_TRY(dalloc(A, &s_.bcon, np), "alloc");
+  LS_TRY(dalloc(A, &s_.bmin, np), "alloc");
+  LS_TRY(dalloc(A, &s_.list0, np), "alloc");
+  LS_TRY(dalloc(A, &s_.list1, np), "alloc");
+  LS_TRY(dalloc(A, &s_.newlist, np), "alloc");
+  LS_TRY(dalloc(A, &s_.nblist, np), "alloc");
+  LS_TRY(dalloc(A, &s_.counts, 8), "alloc");
+  LS_TRY(dalloc(A, &s_.stats, 8), "alloc");
+  LS_TRY(dalloc(A, &d_tmp_, nv), "alloc");
+  LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 8, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 8, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.phi, 0, sizeof(float) * nv, stream_), "memset");
+  LS_TRY(cudaMallocHost((void**)&h_counts_, sizeof(int) * 8), "pinned");
+  LS_TRY(cudaMallocHost((void**)&h_stats_, sizeof(unsigned long long) * 8), "pinned");
+  LS_TRY(cudaMallocHost((void**)&h_stage_, sizeof(float) * nv), "pinned");
+
+  // parameters (FIM quantities in the FIM frame)
+  sp_.largenum = (float)cfg.largenum;
+  sp_.bandwidth = (float)(cfg.bandwidth / scale);
+  sp_.scale = (float)scale;
+  sp_.tau = (cfg.fp64_flagged && L.dim == 3) ? (float)cfg.fp64_tau : 0.f;
+  sp_.tol = (float)cfg.smallnum;
+  sp_.eps_h64 = cfg.smallnum;
+  sp_.eps_h = (float)sp_.eps_h64;
+  sp_.dt = (float)cfg.dt;
+  sp_.curv_coeff = (float)cfg.curv_coeff;
+  sp_.niter = cfg.niter > 0 ? cfg.niter : (L.dim == 3 ? 5 : 10);
+  sp_.ref_compat = ref ? 1 : 0;
+  sp_.update_kind = cfg.update_kind;
+  sp_.lvp = L.lvp;
+  sp_.lgp = L.lgp;
+  sp_.lep = L.lep;
+  (void)d1;
+  LS_TRY(configure_launch(m_, sp_, L_), "configure");
+  if (cfg_.graph_chunk < 2) cfg_.graph_chunk = 2;
+  if (cfg_.graph_chunk & 1) cfg_.graph_chunk++;
+  if (cfg_.use_graph) {
+    std::string r = build_graph();
+    if (!r.empty()) return r;
+  }
+  LS_TRY(cudaStreamSynchronize(stream_), "init sync");
+  return "";
+}
+
+std::string Solver::build_graph() {
+  LS_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
+  cudaError_t err = cudaSuccess;
+  for (int i = 0; i < cfg_.graph_chunk && err == cudaSuccess; ++i) {
+    const int cur = i & 1;
+    err = launch_sweep(m_, s_, sp_, cur, false, L_, stream_);
+    if (err == cudaSuccess) err = launch_schedule(m_, s_, sp_, cur, L_, stream_);
+    if (err == cudaSuccess) err = launch_sweep(m_, s_, sp_, cur, true, L_, stream_);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(stream_, &graph_);
+  LS_TRY(err, "capture launch");
+  LS_TRY(e2, "capture end");
+  LS_TRY(cudaGraphInstantiate(&graph_exec_, graph_, 0), "graph instantiate");
+  return "";
+}
+
+// Profiling helper: event pairs around launches when cfg_.profile is set.
+namespace {
+struct ProfEvent {
+  cudaEvent_t a, b;
+  int kind;
+};
+}  // namespace
+
+static std::vector<ProfEvent>& prof_pending() {
+  static thread_local std::vector<ProfEvent> v;
+  return v;
+}
+
+std::string Solver::fim_loop() {
+  long long launched = 0;
+  auto prof = [&](int kind, auto&& fn) -> cudaError_t {
+    if (!cfg_.profile) return fn();
+    ProfEvent pe;
+    pe.kind = kind;
+    cudaEventCreate(&pe.a);
+    cudaEventCreate(&pe.b);
+    cudaEventRecord(pe.a, stream_);
+    cudaError_t e = fn();
+    cudaEventRecord(pe.b, stream_);
+    prof_pending().push_back(pe);
+    return e;
+  };
+  while (true) {
+    if (graph_exec_ && !cfg_.profile) {
+      LS_TRY(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
+    } else {
+      for (int i = 0; i < cfg_.graph_chunk; ++i) {
+        const int cur = i & 1;
+        LS_TRY(prof(0, [&] { return launch_sweep(m_, s_, sp_, cur, false, L_, stream_); }), "sweep");
+        LS_TRY(prof(2, [&] { return launch_schedule(m_, s_, sp_, cur, L_, stream_); }), "schedule");
+        LS_TRY(prof(1, [&] { return launch_sweep(m_, s_, sp_, cur, true, L_, stream_); }), "check");
+      }
+    }
+    launched += cfg_.graph_chunk;
+    st_.kernel_launches += 3LL * cfg_.graph_chunk;
+    LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaStreamSynchronize(stream_), "fim sync");
+    if (h_counts_[0] == 0) break;
+    if (launched >= cfg_.max_fim_iters) {
+      status_ = 3;
+      return "FIM did not converge within max_fim_iters iterations";
+    }
+  }
+  return "";
+}
+
+std::string Solver::one_step(bool* empty_nb) {
+  *empty_nb = false;
+  auto prof = [&](int kind, auto&& fn) -> cudaError_t {
+    if (!cfg_.profile) return fn();
+    ProfEvent pe;
+    pe.kind = kind;
+    cudaEventCreate(&pe.a);
+    cudaEventCreate(&pe.b);
+    cudaEventRecord(pe.a, stream_);
+    cudaError_t e = fn();
+    cudaEventRecord(pe.b, stream_);
+    prof_pending().push_back(pe);
+    return e;
+  };
+  const int use_all = have_nb_ ? 0 : 1;
+  LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_), "memset");
+  LS_TRY(launch_reset(m_, s_, sp_, L_, stream_), "reset");
+  LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_), "memset");
+  LS_TRY(prof(3, [&] { return launch_seed(m_, s_, use_all, sp_.scale, L_, stream_); }), "seed");
+  LS_TRY(cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_), "memset");
+  st_.kernel_launches += 3;  // reset, seed, narrowband
+  std::string r = fim_loop();
+  if (!r.empty()) return r;
+  LS_TRY(prof(4, [&] { return launch_narrowband(m_, s_, sp_, L_, stream_); }), "narrowband");
+  LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "nb sync");
+  if (h_counts_[3] == 0) {
+    *empty_nb = true;
+    have_nb_ = false;
+    return "";
+  }
+  have_nb_ = true;
+  if (cfg_.update_kind != 2) {
+    for (int it = 0; it < cfg_.inside_niter; ++it) {
+      LS_TRY(prof(5, [&] { return launch_update(m_, s_, sp_, L_, stream_); }), "update");
+      st_.kernel_launches += 2;  // update, copy-back
+    }
+  }
+  return "";
+}
+
+void Solver::pull_stats() {
+  if (cudaMemcpy(h_stats_, s_.stats, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return;
+  st_.patch_visits = (long long)h_stats_[0];
+  st_.check_visits = (long long)h_stats_[1];
+  st_.nb_vertex_updates = (long long)h_stats_[2];
+  st_.nb_patch_vertices = (long long)h_stats_[3];
+  st_.nb_patches = (long long)h_stats_[4];
+  st_.fim_iters = (long long)h_stats_[5];
+  st_.sweep_slab_bytes = (long long)h_stats_[7];
+  st_.flagged_copies = (long long)h_stats_[6];
+  auto& pend = prof_pending();
+  for (auto& pe : pend) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, pe.a, pe.b);
+    switch (pe.kind) {
+      case 0: st_.ms_sweep += ms; st_.n_sweep++; break;
+      case 1: st_.ms_check += ms; st_.n_check++; break;
+      case 2: st_.ms_schedule += ms; st_.n_schedule++; break;
+      case 3: st_.ms_seed += ms; st_.n_seed++; break;
+      case 4: st_.ms_narrowband += ms; st_.n_narrowband++; break;
+      case 5: st_.ms_update += ms; st_.n_update++; break;
+    }
+    cudaEventDestroy(pe.a);
+    cudaEventDestroy(pe.b);
+  }
+  pend.clear();
+}
+
+std::string Solver::run(int nsteps, float* history, int* steps_done) {
+  int done = 0;
+  if (history) {
+    LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+    LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaStreamSynchronize(stream_), "sync");
+    std::memcpy(history, h_stage_, sizeof(float) * m_.nv);
+  }
+  LS_TRY(cudaEventRecord(ev0_, stream_), "event");
+  for (int s = 0; s < nsteps; ++s) {
+    bool empty = false;
+    std::string r = one_step(&empty);
+    if (!r.empty()) return r;
+    if (empty) break;
+    done++;
+    if (history) {
+      LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+      LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
+      LS_TRY(cudaStreamSynchronize(stream_), "sync");
+      std::memcpy(history + (size_t)(s + 1) * m_.nv, h_stage_, sizeof(float) * m_.nv);
+    }
+  }
+  LS_TRY(cudaEventRecord(ev1_, stream_), "event");
+  LS_TRY(cudaEventSynchronize(ev1_), "event sync");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev0_, ev1_);
+  st_.ms_total += ms;
+  st_.steps_run += done;
+  if (steps_done) *steps_done = done;
+  pull_stats();
+  return "";
+}
+
+std::string Solver::step_host(const float* phi_in, float* phi_out) {
+  std::memcpy(h_stage_, phi_in, sizeof(float) * m_.nv);
+  LS_TRY(cudaMemcpyAsync(d_tmp_, h_stage_, sizeof(float) * m_.nv, cudaMemcpyHostToDevice, stream_), "h2d");
+  LS_TRY(launch_permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
+  st_.kernel_launches += 2;  // permute in, unpermute out
+  bool empty = false;
+  std::string r = one_step(&empty);
+  if (!r.empty()) return r;
+  LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+  LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  std::memcpy(phi_out, h_stage_, sizeof(float) * m_.nv);
+  if (!empty) st_.steps_run++;
+  return "";
+}
+
+std::string Solver::set_phi(const float* phi_orig) {
+  std::memcpy(h_stage_, phi_orig, sizeof(float) * m_.nv);
+  LS_TRY(cudaMemcpyAsync(d_tmp_, h_stage_, sizeof(float) * m_.nv, cudaMemcpyHostToDevice, stream_), "h2d");
+  LS_TRY(launch_permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  have_nb_ = false;
+  return "";
+}
+
+std::string Solver::get_phi(float* phi_orig) {
+  LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+  LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  std::memcpy(phi_orig, h_stage_, sizeof(float) * m_.nv);
+  return "";
+}
+
+std::string Solver::narrowband(unsigned char* flags) {
+  LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  const int n = h_counts_[3];
+  std::vector<int> nb(n > 0 ? n : 1);
+  if (n > 0) LS_TRY(cudaMemcpy(nb.data(), s_.nblist, sizeof(int) * n, cudaMemcpyDeviceToHost), "d2h");
+  std::memset(flags, 0, m_.nparts);
+  for (int i = 0; i < n; ++i) flags[nb[i]] = 1;
+  return "";
+}
+
+void Solver::stats(SolverStats& s) const { s = st_; }
+
+void Solver::reset_stats() {
+  st_ = SolverStats();
+  cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 8, stream_);
+  cudaStreamSynchronize(stream_);
+}
+
+}  // namespace lsgb

@@ -1,0 +1,111 @@
+// ls_solver.h -- device solver behind the C ABI: owns the device copy of the
+// patch layout, the step state, the stream and the FIM-iteration graphs.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "ls_device.cuh"
+#include "ls_layout.h"
+
+namespace lsgb {
+
+struct Launch {
+  int sms;
+  int fim_grid, fim_block, fim_smem;
+  int upd_grid, upd_block, upd_smem;
+  int seed_grid;
+  int warp_grid;
+  int flat_grid;
+};
+
+cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L);
+cudaError_t launch_reset(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st);
+cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float scale, const Launch& L, cudaStream_t st);
+cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
+                         const Launch& L, cudaStream_t st);
+cudaError_t launch_schedule(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, const Launch& L,
+                            cudaStream_t st);
+cudaError_t launch_narrowband(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                              cudaStream_t st);
+cudaError_t launch_update(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                          cudaStream_t st);
+cudaError_t launch_unpermute(const DevMesh& m, const float* phi, float* out, const Launch& L, cudaStream_t st);
+cudaError_t launch_permute(const DevMesh& m, const float* in, float* out, const Launch& L, cudaStream_t st);
+
+struct SolverConfig {
+  int update_kind = 0;
+  int ref_compat = 0;
+  int fp64_flagged = 0;
+  int profile = 0;
+  int use_graph = 1;
+  int niter = 0;
+  int inside_niter = 1;
+  int max_fim_iters = 100000;
+  int graph_chunk = 4;
+  double dt = 1.0;
+  double bandwidth = 16.0;
+  double curv_coeff = 1.0;
+  double smallnum = 1e-5;
+  double largenum = 1e9;
+  double length_scale = 0.0;
+  double fp64_tau = 3.814697265625e-06;  // 2^-18
+};
+
+struct SolverStats {
+  long long steps_run = 0;
+  long long fim_iters = 0, patch_visits = 0, check_visits = 0;
+  long long nb_vertex_updates = 0, nb_patch_vertices = 0, nb_patches = 0, flagged_copies = 0;
+  double ms_total = 0;
+  double ms_sweep = 0, ms_check = 0, ms_schedule = 0, ms_seed = 0, ms_narrowband = 0, ms_update = 0;
+  long long n_sweep = 0, n_check = 0, n_schedule = 0, n_seed = 0, n_narrowband = 0, n_update = 0;
+  long long sweep_slab_bytes = 0;
+  long long kernel_launches = 0;
+};
+
+class Solver {
+ public:
+  Solver() = default;
+  ~Solver();
+  // Upload the layout and the per-copy data; phi0 / vel in the caller's order.
+  std::string init(const Layout& L, const SolverConfig& cfg, const float* vel);
+  std::string set_phi(const float* phi_orig);          // host, caller order
+  std::string get_phi(float* phi_orig);                // host, caller order
+  // Run nsteps; history (optional) gets phi after each step (host, caller order).
+  std::string run(int nsteps, float* history, int* steps_done);
+  std::string step_host(const float* phi_in, float* phi_out);
+  std::string narrowband(unsigned char* flags);
+  void stats(SolverStats& s) const;
+  void reset_stats();
+  int status_code() const { return status_; }
+  void set_profile(bool on) { cfg_.profile = on ? 1 : 0; }
+
+ private:
+  std::string check(cudaError_t e, const char* what);
+  std::string one_step(bool* empty_nb);
+  std::string fim_loop();
+  std::string build_graph();
+  void pull_stats();
+
+  const Layout* lay_ = nullptr;
+  SolverConfig cfg_;
+  DevMesh m_{};
+  DevState s_{};
+  StepParams sp_{};
+  Launch L_{};
+  cudaStream_t stream_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  cudaGraph_t graph_ = nullptr;
+  std::vector<void*> allocs_;
+  int* h_counts_ = nullptr;           // pinned mirror of s_.counts
+  unsigned long long* h_stats_ = nullptr;
+  float* h_stage_ = nullptr;          // pinned nv floats
+  float* d_tmp_ = nullptr;            // nv floats (caller-order staging)
+  bool have_nb_ = false;              // previous narrowband valid (seed search restricted)
+  int status_ = 0;
+  SolverStats st_;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+};
+
+}  // namespace lsgb

@@ -1,0 +1,281 @@
+"""ctypes binding of the lsgb300 C ABI (include/lsgb300.h).
+
+The binding is a thin host-side mirror of the reference's LevelSet call
+sequence (src/LevelSet.cu): create, set the mesh, phi and per-element
+velocity, solve, read results.  All compute runs in liblsgb300.so (CUDA,
+sm_103a); loading fails loudly if the library has not been built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblsgb300.so")
+
+LS_OK, LS_BAD_INPUT, LS_PATCH_TOO_LARGE, LS_DEVICE_TIMEOUT, LS_CUDA_ERROR, LS_NOT_READY, LS_NO_MEMORY = range(7)
+UPDATE_ADVECT, UPDATE_CURVATURE, UPDATE_NONE = 0, 1, 2
+REF_COMPAT, FP64_FLAGGED, PROFILE, NO_GRAPH = 1, 2, 4, 8
+
+# reference-format layout arrays (ls_get_layout selectors)
+REF_ARRAYS = {
+    "ele_permute": 0, "ele_offsets": 1, "vert_permute": 2, "vert_offsets": 3,
+    "ele_after_permute": 4, "mem_locations": 5, "mem_location_offsets": 6,
+    "block_xadj": 7, "block_adjncy": 8, "local_coords": 9, "vert_ipermute": 10,
+}
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("num_steps", ctypes.c_int), ("time_step", ctypes.c_double), ("inside_iterations", ctypes.c_int),
+        ("block_size", ctypes.c_int), ("side_lengths", ctypes.c_int), ("bandwidth", ctypes.c_double),
+        ("metis_size", ctypes.c_int), ("partition_type", ctypes.c_int), ("verbose", ctypes.c_int),
+        ("update_kind", ctypes.c_int), ("curv_coeff", ctypes.c_double), ("flags", ctypes.c_uint),
+        ("fim_sweeps", ctypes.c_int), ("max_fim_iters", ctypes.c_int), ("smallnum", ctypes.c_double),
+        ("largenum", ctypes.c_double), ("length_scale", ctypes.c_double), ("fp64_threshold", ctypes.c_double),
+        ("graph_chunk", ctypes.c_int),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("steps_run", ctypes.c_int), ("fim_iters", ctypes.c_longlong), ("patch_visits", ctypes.c_longlong),
+        ("check_visits", ctypes.c_longlong), ("nb_vertex_updates", ctypes.c_longlong),
+        ("nb_patch_vertices", ctypes.c_longlong), ("nb_patches", ctypes.c_longlong),
+        ("flagged_copies", ctypes.c_longlong), ("ms_total", ctypes.c_double),
+        ("ms_sweep", ctypes.c_double), ("ms_check", ctypes.c_double), ("ms_schedule", ctypes.c_double),
+        ("ms_seed", ctypes.c_double), ("ms_narrowband", ctypes.c_double), ("ms_update", ctypes.c_double),
+        ("n_sweep", ctypes.c_longlong), ("n_check", ctypes.c_longlong), ("n_schedule", ctypes.c_longlong),
+        ("n_seed", ctypes.c_longlong), ("n_narrowband", ctypes.c_longlong), ("n_update", ctypes.c_longlong),
+        ("sweep_slab_bytes", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# every entry point declared in include/lsgb300.h
+EXPORTS = [
+    "ls_default_params", "ls_create", "ls_destroy", "ls_set_params", "ls_get_params", "ls_set_mesh",
+    "ls_set_partition", "ls_set_phi", "ls_set_velocity", "ls_prepare", "ls_setup", "ls_solve", "ls_step",
+    "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_narrowband",
+    "ls_get_layout_info", "ls_get_layout", "ls_last_error", "ls_version", "ls_partition_structured",
+    "ls_partition_rcb", "ls_set_profile",
+]
+
+_lib = None
+
+
+def lib():
+    """Load liblsgb300.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("liblsgb300.so not built; run __graft_entry__.build() first (%s)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, F, V = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_void_p
+    L.ls_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.ls_create.argtypes = [ctypes.POINTER(P), I]
+    L.ls_destroy.argtypes = [P]
+    L.ls_set_params.argtypes = [P, ctypes.POINTER(Params)]
+    L.ls_get_params.argtypes = [P, ctypes.POINTER(Params)]
+    L.ls_set_mesh.argtypes = [P, V, I, V, I]
+    L.ls_set_partition.argtypes = [P, V, I]
+    L.ls_set_phi.argtypes = [P, V]
+    L.ls_set_velocity.argtypes = [P, V]
+    L.ls_prepare.argtypes = [P]
+    L.ls_setup.argtypes = [P]
+    L.ls_solve.argtypes = [P, I, V, ctypes.POINTER(I)]
+    L.ls_step.argtypes = [P, I, ctypes.POINTER(I)]
+    L.ls_step_host.argtypes = [P, V, V]
+    L.ls_get_phi.argtypes = [P, V]
+    L.ls_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
+    L.ls_reset_stats.argtypes = [P]
+    L.ls_set_profile.argtypes = [P, I]
+    L.ls_get_narrowband.argtypes = [P, V]
+    L.ls_get_layout_info.argtypes = [P, V]
+    L.ls_get_layout.argtypes = [P, I, V]
+    L.ls_last_error.argtypes = [P]
+    L.ls_last_error.restype = ctypes.c_char_p
+    L.ls_version.restype = ctypes.c_char_p
+    L.ls_partition_structured.argtypes = [I, I, I, I, V, ctypes.POINTER(I)]
+    L.ls_partition_rcb.argtypes = [I, V, I, I, V, ctypes.POINTER(I)]
+    for name in EXPORTS:
+        fn = getattr(L, name)
+        if name not in ("ls_last_error", "ls_version"):
+            fn.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class LevelSetError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("ls status %d: %s" % (code, msg))
+        self.code = code
+
+
+def default_params(**kw):
+    p = Params()
+    lib().ls_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def partition_structured(dim, nside, block, nv):
+    npart = np.zeros(nv, np.int32)
+    n = ctypes.c_int(0)
+    rc = lib().ls_partition_structured(dim, nside, block, nv, _ptr(npart), ctypes.byref(n))
+    if rc:
+        raise LevelSetError(rc, "structured partition")
+    return npart, n.value
+
+
+def partition_rcb(dim, xyz, target):
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    npart = np.zeros(len(xyz), np.int32)
+    n = ctypes.c_int(0)
+    rc = lib().ls_partition_rcb(dim, _ptr(xyz), len(xyz), target, _ptr(npart), ctypes.byref(n))
+    if rc:
+        raise LevelSetError(rc, "rcb partition")
+    return npart, n.value
+
+
+class LevelSet:
+    """Handle over the C ABI.  Same life cycle as the reference LevelSet."""
+
+    def __init__(self, is_tri, params=None):
+        self._h = ctypes.c_void_p()
+        rc = lib().ls_create(ctypes.byref(self._h), 1 if is_tri else 0)
+        if rc:
+            raise LevelSetError(rc, "create")
+        self.is_tri = bool(is_tri)
+        self.nv = 0
+        self.ne = 0
+        if params is not None:
+            self.set_params(params)
+
+    def close(self):
+        if self._h:
+            lib().ls_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != LS_OK:
+            raise LevelSetError(rc, "%s: %s" % (what, lib().ls_last_error(self._h).decode()))
+
+    def set_params(self, p):
+        self._check(lib().ls_set_params(self._h, ctypes.byref(p)), "set_params")
+
+    def set_mesh(self, xyz, elems):
+        self._xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+        self._elems = np.ascontiguousarray(elems, np.int32)
+        self.nv, self.ne = len(self._xyz), len(self._elems)
+        self._check(lib().ls_set_mesh(self._h, _ptr(self._xyz), self.nv, _ptr(self._elems), self.ne), "set_mesh")
+
+    def set_partition(self, npart, nparts):
+        a = np.ascontiguousarray(npart, np.int32)
+        self._check(lib().ls_set_partition(self._h, _ptr(a), int(nparts)), "set_partition")
+
+    def set_phi(self, phi):
+        a = np.ascontiguousarray(phi, np.float32)
+        if self.nv and a.size != self.nv:
+            raise LevelSetError(LS_BAD_INPUT, "Initialize values size does not match number of vertices!")
+        self._check(lib().ls_set_phi(self._h, _ptr(a)), "set_phi")
+
+    def set_velocity(self, vel):
+        a = np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        if self.ne and len(a) != self.ne:
+            raise LevelSetError(LS_BAD_INPUT, "Initialize values size does not match number of elements!")
+        self._check(lib().ls_set_velocity(self._h, _ptr(a)), "set_velocity")
+
+    def prepare(self):
+        self._check(lib().ls_prepare(self._h), "prepare")
+
+    def setup(self):
+        self._check(lib().ls_setup(self._h), "setup")
+
+    def solve(self, nsteps, history=True):
+        hist = np.zeros((nsteps + 1, self.nv), np.float32) if history else None
+        done = ctypes.c_int(0)
+        self._check(lib().ls_solve(self._h, nsteps, _ptr(hist) if hist is not None else None, ctypes.byref(done)),
+                    "solve")
+        return (hist[: done.value + 1] if hist is not None else None), done.value
+
+    def step(self, nsteps=1):
+        done = ctypes.c_int(0)
+        self._check(lib().ls_step(self._h, nsteps, ctypes.byref(done)), "step")
+        return done.value
+
+    def step_host(self, phi_in, phi_out):
+        self._check(lib().ls_step_host(self._h, _ptr(phi_in), _ptr(phi_out)), "step_host")
+
+    def phi(self):
+        out = np.zeros(self.nv, np.float32)
+        self._check(lib().ls_get_phi(self._h, _ptr(out)), "get_phi")
+        return out
+
+    def stats(self):
+        s = Stats()
+        self._check(lib().ls_get_stats(self._h, ctypes.byref(s)), "get_stats")
+        return s.as_dict()
+
+    def set_profile(self, on):
+        self._check(lib().ls_set_profile(self._h, 1 if on else 0), "set_profile")
+
+    def reset_stats(self):
+        self._check(lib().ls_reset_stats(self._h), "reset_stats")
+
+    def narrowband(self, nparts):
+        out = np.zeros(nparts, np.uint8)
+        self._check(lib().ls_get_narrowband(self._h, _ptr(out)), "get_narrowband")
+        return out
+
+    def layout_info(self):
+        info = np.zeros(10, np.int64)
+        self._check(lib().ls_get_layout_info(self._h, _ptr(info)), "layout_info")
+        keys = ["nparts", "full", "lep", "lvp", "lgp", "lim", "nadj", "nv", "ne", "dim"]
+        return dict(zip(keys, (int(x) for x in info)))
+
+    def layout(self, name):
+        info = self.layout_info()
+        d1 = info["dim"] + 1
+        sizes = {
+            "ele_permute": info["full"], "ele_offsets": info["nparts"] + 1, "vert_permute": info["nv"],
+            "vert_ipermute": info["nv"], "vert_offsets": info["nparts"] + 1,
+            "ele_after_permute": d1 * info["full"], "mem_locations": d1 * info["full"],
+            "mem_location_offsets": info["nv"] + 1, "block_xadj": info["nparts"] + 1,
+            "block_adjncy": info["nadj"], "local_coords": (6 if d1 == 4 else 3) * info["full"],
+        }
+        dt = np.float32 if name == "local_coords" else np.int32
+        out = np.zeros(sizes[name], dt)
+        self._check(lib().ls_get_layout(self._h, REF_ARRAYS[name], _ptr(out)), "layout")
+        return out
+
+
+def from_workload(w, ref_compat=False, fp64_flagged=False, profile=False, setup=True, **extra):
+    """LevelSet handle for a synth.workload() dictionary (mesh, partition,
+    phi0, velocity and the step parameters)."""
+    flags = (REF_COMPAT if ref_compat else 0) | (FP64_FLAGGED if fp64_flagged else 0) | (PROFILE if profile else 0)
+    kind = {"advect": UPDATE_ADVECT, "curvature": UPDATE_CURVATURE, "none": UPDATE_NONE}[w["update"]]
+    p = default_params(num_steps=w["steps"], time_step=w["dt"], bandwidth=w["bandwidth"], update_kind=kind,
+                       curv_coeff=1.0, flags=flags, **extra)
+    ls = LevelSet(w["dim"] == 2, p)
+    ls.set_mesh(w["xyz"], w["elems"])
+    ls.set_partition(w["npart"], w["nparts"])
+    ls.set_phi(w["phi0"])
+    ls.set_velocity(w["vel"])
+    if setup:
+        ls.setup()
+    return ls

@@ -1,0 +1,168 @@
+"""Seeded synthetic inputs for the narrowband level-set step.
+
+The reference ships no benchmark inputs (its README lists only demo meshes),
+so the workloads are generated: jittered structured meshes with analytic
+signed-distance initial conditions.
+
+  square: (n+1)^2 vertices on [0,1]^2, two triangles per cell with a fixed
+          diagonal; vertex (i, j) has index j*(n+1) + i (x fastest).
+  cube:   (n+1)^3 vertices on [0,1]^3, Freudenthal split (6 tetrahedra per
+          cell, one per ordering of the three axes); vertex (i, j, k) has
+          index (k*(n+1) + j)*(n+1) + i (x fastest), the numbering of the
+          reference fixture CubeMesh_size256step8_correct.node.
+Interior vertices are jittered uniformly per axis; boundary vertices stay on
+the boundary.
+"""
+import itertools
+
+import numpy as np
+
+
+def square_mesh(n, jitter=0.0, seed=0, scale=1.0):
+    h = 1.0 / n
+    j, i = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    xy = np.stack([i.ravel() * h, j.ravel() * h], 1)
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter * h, jitter * h, size=xy.shape)
+        interior = (i.ravel() > 0) & (i.ravel() < n) & (j.ravel() > 0) & (j.ravel() < n)
+        xy[interior] += d[interior]
+    xyz = np.zeros((len(xy), 3), np.float64)
+    xyz[:, :2] = xy
+    ci, cj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    ci, cj = ci.ravel(), cj.ravel()
+    a = cj * (n + 1) + ci
+    b = a + 1
+    c = a + (n + 1)
+    d = c + 1
+    tris = np.concatenate([np.stack([a, b, d], 1), np.stack([a, d, c], 1)])
+    return (xyz * scale).astype(np.float32), tris.astype(np.int32)
+
+
+def cube_mesh(n, jitter=0.0, seed=0, scale=1.0):
+    h = 1.0 / n
+    N = n + 1
+    k, j, i = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    xyz = np.stack([i * h, j * h, k * h], 1).astype(np.float64)
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter * h, jitter * h, size=xyz.shape)
+        interior = (i > 0) & (i < n) & (j > 0) & (j < n) & (k > 0) & (k < n)
+        xyz[interior] += d[interior]
+    ck, cj, ci = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    ci, cj, ck = ci.ravel(), cj.ravel(), ck.ravel()
+    idx = lambda a, b, c: (c * N + b) * N + a
+    tets = []
+    for perm in itertools.permutations(range(3)):
+        off = np.zeros(3, np.int64)
+        t = [idx(ci, cj, ck)]
+        for ax in perm:
+            off[ax] += 1
+            t.append(idx(ci + off[0], cj + off[1], ck + off[2]))
+        tets.append(np.stack(t, 1))
+    # cell-major order: the six tets of a cell are consecutive
+    tets = np.stack(tets, 1).reshape(-1, 4)
+    return (xyz * scale).astype(np.float32), tets.astype(np.int32)
+
+
+def phi_circle(xyz, center=(0.5, 0.5), r=0.3):
+    p = xyz[:, :2].astype(np.float64) - np.asarray(center)
+    return (np.sqrt((p ** 2).sum(1)) - r).astype(np.float32)
+
+
+def phi_spheres(xyz, centers, radii):
+    p = xyz.astype(np.float64)
+    d = np.full(len(p), np.inf)
+    for c, r in zip(centers, radii):
+        d = np.minimum(d, np.sqrt(((p - np.asarray(c)) ** 2).sum(1)) - r)
+    return d.astype(np.float32)
+
+
+def phi_torus(xyz, center=(0.5, 0.5, 0.5), R=0.3, r=0.1):
+    p = xyz.astype(np.float64) - np.asarray(center)
+    q = np.sqrt(p[:, 0] ** 2 + p[:, 1] ** 2) - R
+    return (np.sqrt(q ** 2 + p[:, 2] ** 2) - r).astype(np.float32)
+
+
+def centroids(xyz, elems):
+    return xyz[elems].astype(np.float64).mean(1)
+
+
+def velocity_rotation(xyz, elems, omega, center=(0.5, 0.5, 0.5), axis=(0.0, 0.0, 1.0)):
+    """Rigid rotation omega * axis x (x - c) evaluated at element centroids."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    x = centroids(xyz, elems) - np.asarray(center)
+    return (omega * np.cross(a, x)).astype(np.float32)
+
+
+def velocity_constant(ne, v):
+    out = np.zeros((ne, 3), np.float32)
+    out[:, : len(v)] = v
+    return out
+
+
+def structured_partition(dim, nside, block):
+    """GraphPartition_Square labels (meshFIM3d.cu:316-326) in numpy."""
+    nb = -(-nside // block)
+    ids = np.arange(nside ** dim)
+    c = [(ids // nside ** a) % nside for a in range(dim)]
+    part = np.zeros(len(ids), np.int64)
+    for a in range(dim):
+        part += (c[a] // block) * nb ** a
+    return part.astype(np.int32), nb ** dim
+
+
+def workload(name, seed=0, scale=1.0, n=None):
+    """The benchmark configurations, as dictionaries of arrays and parameters.
+
+    c1: 2D advection, 64x64 cells, circle r=0.3, velocity (1, 0.5), 20 steps.
+    c2: 3D advection, 32^3 cells, torus R=0.3 r=0.1, rotation about z at 2 pi.
+    c3: 3D mean-curvature flow, 128^3 cells, union of 3 spheres, dt = 0.5 h^2.
+    `n` overrides the cells per side (smaller cases of the same family);
+    `scale` multiplies coordinates (lengths, dt and the bandwidth follow).
+    """
+    rng = np.random.default_rng(1000 + seed)
+    if name == "c1":
+        n = n or 64
+        h = 1.0 / n
+        xyz, el = square_mesh(n, 0.2, seed)
+        phi = phi_circle(xyz)
+        vel = velocity_constant(len(el), (1.0, 0.5))
+        spd = np.sqrt(1.0 + 0.25)
+        npart, nparts = structured_partition(2, n + 1, 5)
+        cfg = dict(dim=2, steps=20, dt=0.5 * h / spd, bandwidth=5 * h, update="advect", block=5)
+    elif name == "c2":
+        n = n or 32
+        h = 1.0 / n
+        xyz, el = cube_mesh(n, 0.15, seed)
+        phi = phi_torus(xyz)
+        vel = velocity_rotation(xyz, el, 2 * np.pi)
+        vmax = float(np.sqrt((vel.astype(np.float64) ** 2).sum(1)).max())
+        npart, nparts = structured_partition(3, n + 1, 3)
+        cfg = dict(dim=3, steps=100, dt=0.5 * h / vmax, bandwidth=5 * h, update="advect", block=3)
+    elif name == "c3":
+        n = n or 128
+        h = 1.0 / n
+        xyz, el = cube_mesh(n, 0.15, seed)
+        centers = rng.uniform(0.25, 0.75, size=(3, 3))
+        radii = rng.uniform(0.1, 0.25, size=3)
+        phi = phi_spheres(xyz, centers, radii)
+        vel = np.zeros((len(el), 3), np.float32)
+        npart, nparts = structured_partition(3, n + 1, 3)
+        cfg = dict(dim=3, steps=50, dt=0.5 * h * h, bandwidth=6 * h, update="curvature", block=3,
+                   centers=centers, radii=radii)
+    else:
+        raise ValueError(name)
+    cfg.update(name=name, n=n, h=h * scale, seed=seed)
+    if scale != 1.0:
+        xyz = (xyz.astype(np.float64) * scale).astype(np.float32)
+        phi = (phi.astype(np.float64) * scale).astype(np.float32)
+        cfg["bandwidth"] *= scale
+        if cfg["update"] == "curvature":
+            cfg["dt"] *= scale * scale
+        else:
+            vel = (vel.astype(np.float64) * scale).astype(np.float32)
+            cfg["dt"] *= 1.0
+    return dict(xyz=xyz, elems=el, phi0=phi, vel=vel, npart=npart, nparts=nparts, **cfg)
