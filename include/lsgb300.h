@@ -67,7 +67,11 @@ enum {
   /* Record per-kernel CUDA-event timings (ls_get_stats). */
   LS_PROFILE = 1u << 2,
   /* Do not use CUDA graphs for the FIM iteration chunks. */
-  LS_NO_GRAPH = 1u << 3
+  LS_NO_GRAPH = 1u << 3,
+  /* Use the bit-exact kernel build (no FMA contraction; every float
+   * operation individually rounded in the reference's order).  Slower;
+   * reproduces the CPU restatement of the reference bit for bit. */
+  LS_BITEXACT = 1u << 4
 };
 
 typedef struct ls_params {

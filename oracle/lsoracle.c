@@ -53,7 +53,7 @@ int lso_version(void) { return 1; }
  * the double literals make them in the reference. */
 static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
                           float ACCD, float BCBC, float BCCD, float CDCD,
-                          double eps_h, float LN, float tau, int* ill) {
+                          double eps_h, float LN, float tau, int* ill, int fdiv) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
   float p, q, r, lambda1, lambda2, lambda3;
   float FaceTAC = LN, FaceTAB = LN, FaceTBC = LN;
@@ -152,7 +152,8 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
     lambda1 = (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
-    lambda2 = (float)((double)(s * lambda1 + t) / ((double)h + eps_h));
+    lambda2 = fdiv ? (s * lambda1 + t) / (h + (float)eps_h)
+                   : (float)((double)(s * lambda1 + t) / ((double)h + eps_h));
     lambda3 = 1 - lambda1 - lambda2;
     if (lambda1 >= 0 && lambda1 <= 1 && lambda2 >= 0 && lambda2 <= 1 && lambda3 >= 0 && lambda3 <= 1) {
       TE = TA * lambda1 + TB * lambda2 + TC * lambda3;
@@ -161,7 +162,8 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
                                 (lambda1 * ACCD + lambda2 * BCCD + CDCD)));
     }
     lambda1 = (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
-    lambda2 = (float)((double)(s * lambda1 + t) / ((double)h + eps_h));
+    lambda2 = fdiv ? (s * lambda1 + t) / (h + (float)eps_h)
+                   : (float)((double)(s * lambda1 + t) / ((double)h + eps_h));
     lambda3 = 1 - lambda1 - lambda2;
     if (lambda1 >= 0 && lambda1 <= 1 && lambda2 >= 0 && lambda2 <= 1 && lambda3 >= 0 && lambda3 <= 1) {
       TE = TA * lambda1 + TB * lambda2 + TC * lambda3;
@@ -177,7 +179,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
 float lso_tet_solve_f32(float TA, float TB, float TC, float ACAC, float ACBC,
                         float ACCD, float BCBC, float BCCD, float CDCD,
                         double eps_h, float LN) {
-  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL);
+  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL, 0);
 }
 
 /* The same solver with every quantity in double (the FP64 oracle). */
@@ -267,11 +269,21 @@ double lso_tet_solve_f64(double TA, double TB, double TC, double ACAC,
   return TD;
 }
 
+static float tet_f32_flagged(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                             float BCBC, float BCCD, float CDCD, double eps_h, float LN, float tau,
+                             int* flagged, int fdiv) {
+  int ill = 0;
+  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill, fdiv);
+  if (flagged) *flagged = ill;
+  if (!ill) return r;
+  return (float)lso_tet_solve_f64(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
+}
+
 float lso_tet_solve_f32_flagged(float TA, float TB, float TC, float ACAC, float ACBC,
                                 float ACCD, float BCBC, float BCCD, float CDCD,
                                 double eps_h, float LN, float tau, int* flagged) {
   int ill = 0;
-  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill);
+  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill, 0);
   if (flagged) *flagged = ill;
   if (!ill) return r;
   return (float)lso_tet_solve_f64(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
@@ -298,11 +310,14 @@ static void copy_coords_f32(const lso_layout* lo, const struct ctx_f32* cx, int 
   int nc = lo->dim == 3 ? 6 : 3;
   for (int i = 0; i < nc; ++i) L[i] = cx->lc[(size_t)c * nc + i];
 }
+/* fdiv: without the reference's semantics the interior division
+ * (s l1 + t) / (h + SMALLNUM) is evaluated in float (the GPU does the same);
+ * with them, in double as the reference's double SMALLNUM makes it. */
 static float tet_f32(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD, float BCBC,
-                     float BCCD, float CDCD, double eps_h, float LN, double tau) {
+                     float BCCD, float CDCD, double eps_h, float LN, double tau, int fdiv) {
   if (tau > 0)
-    return lso_tet_solve_f32_flagged(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, (float)tau, NULL);
-  return lso_tet_solve_f32(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
+    return tet_f32_flagged(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, (float)tau, NULL, fdiv);
+  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL, fdiv);
 }
 #include "lso_real.inc"
 #undef REAL
@@ -332,8 +347,9 @@ static void copy_coords_f64(const lso_layout* lo, const struct ctx_f64* cx, int 
   for (int i = 0; i < nc; ++i) L[i] = cx->lc[(size_t)c * nc + i];
 }
 static double tet_f64(double TA, double TB, double TC, double ACAC, double ACBC, double ACCD,
-                      double BCBC, double BCCD, double CDCD, double eps_h, double LN, double tau) {
+                      double BCBC, double BCCD, double CDCD, double eps_h, double LN, double tau, int fdiv) {
   (void)tau;
+  (void)fdiv;
   return lso_tet_solve_f64(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
 }
 #include "lso_real.inc"

@@ -16,7 +16,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblsgb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["ls_layout.cpp", "ls_api.cpp", "ls_solver.cu", "ls_kernels.cu"]
+SOURCES = ["ls_layout.cpp", "ls_api.cpp", "ls_solver.cu", "ls_kernels.cu", "ls_kernels_exact.cu"]
+# translation units compiled without FMA contraction
+NO_FMA = {"ls_kernels_exact.cu"}
 
 
 def nvcc():
@@ -33,7 +35,10 @@ def _run(cmd):
 
 def build(verbose=False, ptxas_info=False):
     os.makedirs(OUT, exist_ok=True)
-    flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I" + os.path.join(HERE, "..", "include")] + ARCH
+    # host code without FP contraction: the host-side local coordinates must
+    # round exactly like the CPU oracle's on x86 and Arm alike
+    flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+             "-I" + os.path.join(HERE, "..", "include")] + ARCH
     if ptxas_info:
         flags += ["-Xptxas", "-v"]
     jobs = []
@@ -41,7 +46,8 @@ def build(verbose=False, ptxas_info=False):
     for src in SOURCES:
         obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
-        jobs.append([nvcc()] + flags + ["-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj])
+        extra = ["-fmad=false"] if src in NO_FMA else []
+        jobs.append([nvcc()] + flags + extra + ["-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(_run, jobs))
     _run([nvcc(), "-shared"] + ARCH + objs + ["-o", LIB])

@@ -276,6 +276,7 @@ ls_status ls_setup(ls_handle* h) {
   cfg.fp64_flagged = (p.flags & LS_FP64_FLAGGED) ? 1 : 0;
   cfg.profile = (p.flags & LS_PROFILE) ? 1 : 0;
   cfg.use_graph = (p.flags & LS_NO_GRAPH) ? 0 : 1;
+  cfg.bit_exact = (p.flags & LS_BITEXACT) ? 1 : 0;
   cfg.niter = p.fim_sweeps;
   cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
   cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;

@@ -61,6 +61,7 @@ struct StepParams {
   float bandwidth;   // in the FIM frame (divided by scale)
   float scale;       // FIM frame length unit (1 with the reference's semantics)
   float tau;         // precision form: discriminant cancellation threshold
+  int xdiv;          // interior division in double (bit-exact build, reference semantics)
   float tol;       // convergence threshold on oldT - newT
   float eps_h;     // denominator offset of the interior tet update
   double eps_h64;
@@ -80,19 +81,26 @@ template <>
 __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a, b); }
 
 // Unit-speed tet update of vertex D from face ABC given the metric terms of
-// the edge vectors AC, BC, CD (R = float or double).
+// the edge vectors AC, BC, CD (R = float or double).  Every expression keeps
+// the reference's operand order and association, so that a build without
+// FMA contraction reproduces the reference arithmetic bit for bit.
+//
+// XDIV: the reference evaluates the interior barycentric coordinate
+// `(s * l1 + t) / (h + SMALLNUM)` with a double SMALLNUM, i.e. in double;
+// XDIV = true reproduces that (used only by the bit-exact build with the
+// reference's semantics), XDIV = false divides in R.
 //
 // `tau` > 0 turns on the conditioning check of the precision form: `ill` is
 // set when a discriminant q^2 - 4pr cancels, |q^2 - 4pr| <= tau (q^2 + |4pr|),
 // i.e. when FP32 has lost about log2(1/tau) bits of it.
-template <typename R>
+template <typename R, bool XDIV>
 __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD, R BCBC, R BCCD,
-                                       R CDCD, R eps_h, R LN, R tau, bool& ill) {
+                                       R CDCD, R eps_h, double eps_h64, R LN, R tau, bool& ill) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
-  R p, q, r, l1, l2, l3, delta, TE;
+  const R two = R(2), four = R(4), one = R(1), zero = R(0);
+  R p, q, r, lambda1, lambda2, lambda3, delta, TE;
   R FaceTAC = LN, FaceTAB = LN, FaceTBC = LN, TD = LN;
   const R TAC = TC - TA, TBC = TC - TB, TAB = TB - TA;
-  const R two = R(2), four = R(4), one = R(1), zero = R(0);
 
   // face BC (lambda1 = 0)
   p = BCBC * TBC * TBC - BCBC * BCBC;
@@ -102,62 +110,63 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
-    l2 = (-q + sq) / (two * p);
-    l3 = one - zero - l2;
-    if (l2 >= zero && l2 <= one) {
-      TE = TB * l2 + TC * l3;
-      FaceTBC = rmin(FaceTBC, TE + sqrt((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD)));
+    lambda1 = zero;
+    lambda2 = (-q + sq) / (two * p);
+    lambda3 = one - lambda1 - lambda2;
+    if (lambda2 >= zero && lambda2 <= one) {
+      TE = TB * lambda2 + TC * lambda3;
+      FaceTBC = rmin(FaceTBC, TE + sqrt((lambda2 * BCBC + BCCD) * lambda2 + (lambda2 * BCCD + CDCD)));
     }
-    l2 = (-q - sq) / (two * p);
-    l3 = one - zero - l2;
-    if (l2 >= zero && l2 <= one) {
-      TE = TB * l2 + TC * l3;
-      FaceTBC = rmin(FaceTBC, TE + sqrt((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD)));
+    lambda2 = (-q - sq) / (two * p);
+    lambda3 = one - lambda1 - lambda2;
+    if (lambda2 >= zero && lambda2 <= one) {
+      TE = TB * lambda2 + TC * lambda3;
+      FaceTBC = rmin(FaceTBC, TE + sqrt((lambda2 * BCBC + BCCD) * lambda2 + (lambda2 * BCCD + CDCD)));
     }
   }
   FaceTBC = rmin(FaceTBC, rmin(TB + sqrt((BCBC + BCCD) + (BCCD + CDCD)), TC + sqrt(CDCD)));
 
   // face AB (lambda3 = 0)
-  const R gx = ACAC - ACBC, gy = ACBC - BCBC, gz = ACCD - BCCD;
-  const R TAB2 = TAB * TAB;
-  p = (TAB2 * ACAC - gx * gx) + (BCBC * TAB2 - gy * gy) - ((ACBC + ACBC) * TAB2 - two * gx * gy);
-  q = -(BCBC * TAB2 - gy * gy) * two + ((ACBC + ACBC) * TAB2 - two * gx * gy) +
-      ((ACCD + ACCD) * TAB2 - two * gx * gz) - ((BCCD + BCCD) * TAB2 - two * gy * gz);
-  r = (TAB2 * BCBC - gy * gy) + ((BCCD + BCCD) * TAB2 - two * gy * gz) + (TAB2 * CDCD - gz * gz);
+  const R gammax = ACAC - ACBC, gammay = ACBC - BCBC, gammaz = ACCD - BCCD;
+  p = (TAB * TAB * ACAC - gammax * gammax) + (BCBC * TAB * TAB - gammay * gammay) -
+      ((ACBC + ACBC) * TAB * TAB - two * gammax * gammay);
+  q = -(BCBC * TAB * TAB - gammay * gammay) * two + ((ACBC + ACBC) * TAB * TAB - two * gammax * gammay) +
+      ((ACCD + ACCD) * TAB * TAB - two * gammax * gammaz) - ((BCCD + BCCD) * TAB * TAB - two * gammay * gammaz);
+  r = (TAB * TAB * BCBC - gammay * gammay) + ((BCCD + BCCD) * TAB * TAB - two * gammay * gammaz) +
+      (TAB * TAB * CDCD - gammaz * gammaz);
   delta = q * q - four * p * r;
   ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      l1 = (-q + (sgn ? -sq : sq)) / (two * p);
-      l2 = one - l1;
-      if (l1 >= zero && l1 <= one) {
-        TE = TA * l1 + TB * l2;
-        FaceTAB = rmin(FaceTAB, TE + sqrt((l1 * ACAC + l2 * ACBC + ACCD) * l1 +
-                                          (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                                          (l1 * ACCD + l2 * BCCD + CDCD)));
+      lambda1 = (-q + (sgn ? -sq : sq)) / (two * p);
+      lambda2 = one - lambda1;
+      if (lambda1 >= zero && lambda1 <= one) {
+        TE = TA * lambda1 + TB * lambda2;
+        FaceTAB = rmin(FaceTAB, TE + sqrt((lambda1 * ACAC + lambda2 * ACBC + ACCD) * lambda1 +
+                                          (lambda1 * ACBC + lambda2 * BCBC + BCCD) * lambda2 +
+                                          (lambda1 * ACCD + lambda2 * BCCD + CDCD)));
       }
     }
   }
   FaceTAB = rmin(FaceTAB, rmin(TB + sqrt((BCBC + BCCD) + (BCCD + CDCD)), TA + sqrt((ACAC + ACCD) + (ACCD + CDCD))));
 
   // face AC (lambda2 = 0)
-  const R TAC2 = TAC * TAC;
-  p = ACAC * TAC2 - ACAC * ACAC;
-  q = (ACCD + ACCD) * TAC2 - two * ACAC * ACCD;
-  r = TAC2 * CDCD - ACCD * ACCD;
+  p = ACAC * TAC * TAC - ACAC * ACAC;
+  q = (ACCD + ACCD) * TAC * TAC - two * ACAC * ACCD;
+  r = TAC * TAC * CDCD - ACCD * ACCD;
   delta = q * q - four * p * r;
   ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      l1 = (-q + (sgn ? -sq : sq)) / (two * p);
-      l3 = one - l1 - zero;
-      if (l1 >= zero && l1 <= one) {
-        TE = TA * l1 + TC * l3;
-        FaceTAC = rmin(FaceTAC, TE + sqrt((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD)));
+      lambda1 = (-q + (sgn ? -sq : sq)) / (two * p);
+      lambda3 = one - lambda1 - zero;
+      if (lambda1 >= zero && lambda1 <= one) {
+        TE = TA * lambda1 + TC * lambda3;
+        FaceTAC = rmin(FaceTAC, TE + sqrt((lambda1 * ACAC + ACCD) * lambda1 + (lambda1 * ACCD + CDCD)));
       }
     }
   }
@@ -167,29 +176,30 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   const R s = TAC * ACBC - TBC * ACAC;
   const R t = TAC * BCCD - TBC * ACCD;
   const R h = -(TAC * BCBC - TBC * ACBC);
-  const R cA = TAC2 * ACAC - ACAC * ACAC;
-  const R cB = BCBC * TAC2 - ACBC * ACBC;
-  const R cC = (ACBC + ACBC) * TAC2 - two * ACAC * ACBC;
-  const R cD = (ACCD + ACCD) * TAC2 - two * ACAC * ACCD;
-  const R cE = (BCCD + BCCD) * TAC2 - two * ACBC * ACCD;
-  const R cF = TAC2 * CDCD - ACCD * ACCD;
-  p = cA * h * h + cB * s * s + cC * s * h;
-  q = cB * two * s * t + cC * t * h + cD * h * h + cE * s * h;
-  r = cB * t * t + cE * t * h + cF * h * h;
+  p = (TAC * TAC * ACAC - ACAC * ACAC) * h * h + (BCBC * TAC * TAC - ACBC * ACBC) * s * s +
+      ((ACBC + ACBC) * TAC * TAC - two * ACAC * ACBC) * s * h;
+  q = (BCBC * TAC * TAC - ACBC * ACBC) * two * s * t + ((ACBC + ACBC) * TAC * TAC - two * ACAC * ACBC) * t * h +
+      ((ACCD + ACCD) * TAC * TAC - two * ACAC * ACCD) * h * h + ((BCCD + BCCD) * TAC * TAC - two * ACBC * ACCD) * s * h;
+  r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - two * ACBC * ACCD) * t * h +
+      (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
   delta = q * q - four * p * r;
   ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
-    const R hd = h + eps_h;
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      l1 = (-q + (sgn ? -sq : sq)) / (two * p);
-      l2 = (s * l1 + t) / hd;
-      l3 = one - l1 - l2;
-      if (l1 >= zero && l1 <= one && l2 >= zero && l2 <= one && l3 >= zero && l3 <= one) {
-        TE = TA * l1 + TB * l2 + TC * l3;
-        TD = rmin(TD, TE + sqrt((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                                (l1 * ACCD + l2 * BCCD + CDCD)));
+      lambda1 = (-q + (sgn ? -sq : sq)) / (two * p);
+      if (XDIV)
+        lambda2 = (R)((double)(s * lambda1 + t) / ((double)h + eps_h64));
+      else
+        lambda2 = (s * lambda1 + t) / (h + eps_h);
+      lambda3 = one - lambda1 - lambda2;
+      if (lambda1 >= zero && lambda1 <= one && lambda2 >= zero && lambda2 <= one && lambda3 >= zero &&
+          lambda3 <= one) {
+        TE = TA * lambda1 + TB * lambda2 + TC * lambda3;
+        TD = rmin(TD, TE + sqrt((lambda1 * ACAC + lambda2 * ACBC + ACCD) * lambda1 +
+                                (lambda1 * ACBC + lambda2 * BCBC + BCCD) * lambda2 +
+                                (lambda1 * ACCD + lambda2 * BCCD + CDCD)));
       }
     }
   }
@@ -197,18 +207,19 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   return TD;
 }
 
-// Triangle update of C from edge AB; square roots in single precision as in
-// the reference (which passes doubles to sqrtf).
+// Triangle update of C from edge AB (speed 1); the square roots are taken in
+// single precision as in the reference, which passes doubles to sqrtf.
 template <typename R>
 __device__ __forceinline__ R tri_solve(R TA, R TB, R LenAB, R LenBC, R LenAC, R LN) {
   if (TA >= LN && TB >= LN) return LN;
+  const R speedI = R(1);
   const R TAB = TB - TA;
-  const R a = (LenAB * LenAB - TAB * TAB) * LenAB * LenAB;
-  const R EdgeTA = TA + LenAC, EdgeTB = TB + LenBC;
+  const R a = (speedI * speedI * LenAB * LenAB - TAB * TAB) * LenAB * LenAB;
+  const R EdgeTA = TA + LenAC * speedI, EdgeTB = TB + LenBC * speedI;
   R TC1 = LN, TC2 = LN;
   if (a > R(0)) {
     const R cosA = (LenAC * LenAC + LenAB * LenAB - LenBC * LenBC) / (R(2) * LenAC * LenAB);
-    const R b = R(2) * LenAB * LenAC * cosA * (TAB * TAB - LenAB * LenAB);
+    const R b = R(2) * LenAB * LenAC * cosA * (TAB * TAB - speedI * speedI * LenAB * LenAB);
     const R delta = R(4) * LenAC * LenAC * a * TAB * TAB * (R(1) - cosA * cosA);
     const R sq = (R)sqrtf((float)delta);
     const R l1 = (-b + sq) / (R(2) * a);
@@ -216,12 +227,12 @@ __device__ __forceinline__ R tri_solve(R TA, R TB, R LenAB, R LenBC, R LenAC, R 
     if (l1 >= R(0) && l1 <= R(1)) {
       const R LenAD = l1 * LenAB;
       const R LenCD = (R)sqrtf((float)(LenAC * LenAC + LenAD * LenAD - R(2) * LenAC * LenAD * cosA));
-      TC1 = l1 * TAB + TA + LenCD;
+      TC1 = l1 * TAB + TA + LenCD * speedI;
     }
     if (l2 >= R(0) && l2 <= R(1)) {
       const R LenAD = l2 * LenAB;
       const R LenCD = (R)sqrtf((float)(LenAC * LenAC + LenAD * LenAD - R(2) * LenAC * LenAD * cosA));
-      TC2 = l2 * TAB + TA + LenCD;
+      TC2 = l2 * TAB + TA + LenCD * speedI;
     }
     return rmin(TC2, rmin(TC1, rmin(EdgeTA, EdgeTB)));
   }

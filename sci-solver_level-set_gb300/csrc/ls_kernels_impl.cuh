@@ -1,0 +1,756 @@
+// ls_kernels_impl.cuh -- sm_103a kernels of the narrowband level-set time step.
+// Included twice: by ls_kernels.cu (fast build, FMA contraction on) and by
+// ls_kernels_exact.cu (compiled with -fmad=false; with the same operand
+// order as the CPU oracle it reproduces the oracle bit for bit).
+//
+// One step (reference order, src/core3d/cuda/meshFIM3d.cu:639-678):
+//   k_reset        DT := LARGENUM, seed := 0, sign := (phi >= 0)     (whole mesh)
+//   k_seed         seed points and the first active patch list        (K9)
+//   FIM iterations, each:
+//     k_fim<SWEEP> NITER sweeps on every active patch, fused per-patch
+//                  convergence AND and min (K11 + K13)
+//     k_schedule   copy-back, unconverged patches to the next list,
+//                  neighbours of converged patches with min < w to the
+//                  candidate list (the host loop of redistance3d.cu:139-181)
+//     k_fim<CHECK> one-sweep probe of the candidates; unconverged ones join
+//                  the next list (K12 + K13 + redistance3d.cu:188-222)
+//   k_narrowband   patch narrowband, phi := sign * DT, vertex-update count (K14 + K10b)
+//   k_update       advection (K16) or mean-curvature update on narrowband patches
+//   k_copy_phi     phi := phi_out on narrowband patches (K15)
+//   k_unpermute    phi in the caller's vertex order (K18)
+//
+// Patch visits read a contiguous slab: owned vertex values [vs, ve) plus a
+// sorted ghost list, 16-bit slab-local connectivity (one 8-byte load per
+// element copy), SoA local coordinates.  The per-vertex minimum of the
+// reference's gather/broadcast (redistance_kernels3d.h:418-436) is a shared-
+// memory atomicMin on the float bit pattern (values are non-negative), and
+// ghost values stay private to each element copy, as in the reference.
+
+
+__device__ __forceinline__ int warp_id_global() {
+  return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_reset(DevState s, int nv, float LN) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    s.DT[v] = LN;
+    s.seed[v] = 0;
+    s.sign[v] = (s.phi[v] < 0.f) ? 0 : 1;
+  }
+}
+
+// Seed search (redistance_kernels3d.h:623-770): an element copy whose
+// vertex values include an exact zero or differ in sign marks those
+// vertices as seeds with DT = |phi|; the patch joins list0.
+template <int D1>
+__global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
+  const int count = use_all ? m.nparts : s.counts[3];
+  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+    const int p = use_all ? li : s.nblist[li];
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    const int gs = m.ghost_off[p];
+    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+    int found = 0;
+    for (int c = threadIdx.x; c < nep; c += blockDim.x) {
+      const ushort4 cv = m.conn[es + c];
+      const int idx[4] = {cv.x, cv.y, cv.z, cv.w};
+      int gv[D1];
+      float val[D1];
+      bool allpos = true, allneg = true;
+#pragma unroll
+      for (int k = 0; k < D1; ++k) {
+        gv[k] = idx[k] < nvp ? vs + idx[k] : m.ghost_ids[gs + idx[k] - nvp];
+        val[k] = s.phi[gv[k]];
+        allpos &= (val[k] >= 0.f);
+        allneg &= (val[k] <= 0.f);
+      }
+      const bool cross = !(allpos || allneg);
+#pragma unroll
+      for (int k = 0; k < D1; ++k) {
+        if (cross || val[k] == 0.f) {
+          s.seed[gv[k]] = 1;
+          s.DT[gv[k]] = fabsf(val[k]) / scale;
+          found = 1;
+        }
+      }
+    }
+    found = __syncthreads_or(found);
+    if (threadIdx.x == 0 && found) {
+      const int pos = atomicAdd(&s.counts[0], 1);
+      s.list0[pos] = p;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FIM patch visit.  CHECK = false: NITER sweeps, writes DT_out and the patch
+// convergence / minimum / label (kernel_update_values + run_reduction_
+// bandwidth).  CHECK = true: one sweep, no value writes; unconverged
+// candidates are appended to the next list (kernel_run_check_neghbor +
+// run_reduction3d + redistance3d.cu:214-222).
+// Solves of one element copy (Jacobi: all from the values at sweep start).
+// With the precision form (tau > 0) a solve whose discriminant cancelled is
+// repeated in FP64; `nflag` counts those repeats.
+template <int D1, bool XDIV>
+__device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], float out[4], float eps_h,
+                                           double eps_h64, float LN, float tau, int& nflag) {
+  if (D1 == 4) {
+    const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4];
+    const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
+    const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
+    bool ill[4] = {false, false, false, false};
+    float r3 = tet_solve<float, XDIV>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3]);
+    float r0 = tet_solve<float, XDIV>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0]);
+    float r1 = tet_solve<float, XDIV>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1]);
+    float r2 = tet_solve<float, XDIV>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2]);
+    if (tau > 0.f && (ill[0] | ill[1] | ill[2] | ill[3])) {
+      const double L64 = LN;
+      bool d = false;
+      if (ill[3]) { r3 = (float)tet_solve<double, false>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[0]) { r0 = (float)tet_solve<double, false>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[1]) { r1 = (float)tet_solve<double, false>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[2]) { r2 = (float)tet_solve<double, false>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+    }
+    out[3] = fminf(TD, r3);
+    out[0] = fminf(TA, r0);
+    out[1] = fminf(TB, r1);
+    out[2] = fminf(TC, r2);
+  } else {
+    const float LenAB = Mt[0], LenBC = Mt[1], LenCA = Mt[2];
+    const float TA = T[0], TB = T[1], TC = T[2];
+    out[2] = fminf(TC, tri_solve<float>(TA, TB, LenAB, LenBC, LenCA, LN));
+    out[0] = fminf(TA, tri_solve<float>(TB, TC, LenBC, LenCA, LenAB, LN));
+    out[1] = fminf(TB, tri_solve<float>(TC, TA, LenCA, LenAB, LenBC, LN));
+    out[3] = LN;
+  }
+}
+
+template <int D1>
+__device__ __forceinline__ void copy_metric(const DevMesh& m, long long c, float* Mt) {
+  const long long F = m.full;
+  if (D1 == 4) {
+    float L[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) L[i] = __ldg(m.lc + i * F + c);
+    // redistance_kernels3d.h:381-396
+    const float ACBC = L[1] * (L[1] - L[0]) + L[2] * L[2];
+    const float BCCD = (L[1] - L[0]) * (L[3] - L[1]) + L[2] * (L[4] - L[2]);
+    const float ACCD = L[1] * (L[3] - L[1]) + L[2] * (L[4] - L[2]);
+    const float ADBD = L[3] * (L[3] - L[0]) + L[4] * L[4] + L[5] * L[5];
+    const float ACAD = L[1] * L[3] + L[2] * L[4];
+    const float BCBD = (L[1] - L[0]) * (L[3] - L[0]) + L[2] * L[4];
+    const float ADBC = ACBC + BCCD;
+    const float ACBD = ACBC + ACCD;
+    const float CDBD = ADBD - ACBD;
+    const float ADCD = ADBD - ADBC;
+    const float CDCD = ADCD - ACCD;
+    Mt[0] = ACAD - ACCD;   // ACAC
+    Mt[1] = ACBC;
+    Mt[2] = ACCD;
+    Mt[3] = BCBD - BCCD;   // BCBC
+    Mt[4] = BCCD;
+    Mt[5] = CDCD;
+    Mt[6] = ADCD + ACAD;   // ADAD
+    Mt[7] = ADBD;
+    Mt[8] = ADCD;
+    Mt[9] = BCBD + CDBD;   // BDBD
+    Mt[10] = CDBD;
+  } else {
+    const float c0 = __ldg(m.lc + c), c1 = __ldg(m.lc + F + c), c2 = __ldg(m.lc + 2 * F + c);
+    Mt[0] = fabsf(c0);
+    Mt[1] = sqrtf(c2 * c2 + (c1 - c0) * (c1 - c0));
+    Mt[2] = sqrtf(c1 * c1 + c2 * c2);
+  }
+}
+
+// The neighbour check and the sweep are one kernel with a runtime flag: both
+// must evaluate a patch's first sweep with the same instructions, otherwise
+// differently contracted FMAs could make the check report a drop of more
+// than the tolerance that the following visit never applies, and two
+// patches could re-activate each other without end.
+template <int D1, int MAXT, bool XDIV>
+__global__ void __launch_bounds__(MAXT) k_fim(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+  const bool CHECK = check != 0;
+  extern __shared__ float smem[];
+  float* sT = smem;                       // owned + ghost values
+  float* sOld = smem + sp.lvp + sp.lgp;   // owned values at the start of the last sweep
+  __shared__ unsigned s_min;
+  const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
+  const int count = CHECK ? s.counts[2] : s.counts[cur];
+  const int nxt = cur ^ 1;
+  int* nlist = nxt ? s.list1 : s.list0;
+  if (!CHECK && blockIdx.x == 0 && threadIdx.x == 0) {
+    // the next list and the candidate list are filled by the following kernels
+    s.counts[nxt] = 0;
+    s.counts[2] = 0;
+    if (count > 0) {
+      s.counts[4] += 1;
+      atomicAdd(&s.stats[5], 1ull);
+    }
+    atomicAdd(&s.stats[0], (unsigned long long)count);
+  }
+  if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
+  const int niter = CHECK ? 1 : sp.niter;
+  const int tid = threadIdx.x;
+  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+    const int p = list[li];
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
+    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+    for (int i = tid; i < nvp + ngp; i += blockDim.x)
+      sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
+    if (tid == 0) s_min = 0x7f800000u;
+    __syncthreads();
+    const bool act = tid < nep;
+    int idx[4] = {0, 0, 0, 0};
+    float T[4] = {0.f, 0.f, 0.f, 0.f};
+    float Mt[11];
+    int nflag = 0;
+    if (act) {
+      const ushort4 cv = m.conn[es + tid];
+      idx[0] = cv.x; idx[1] = cv.y; idx[2] = cv.z; idx[3] = cv.w;
+#pragma unroll
+      for (int k = 0; k < D1; ++k) T[k] = sT[idx[k]];
+      copy_metric<D1>(m, (long long)es + tid, Mt);
+    }
+#pragma unroll 1
+    for (int it = 0; it < niter; ++it) {
+      if (it == niter - 1) {
+        for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
+        __syncthreads();
+      }
+      if (act) {
+        float nw[4];
+        solve_copy<D1, XDIV>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau, nflag);
+#pragma unroll
+        for (int k = 0; k < D1; ++k) {
+          if (idx[k] < nvp) atomicMin(reinterpret_cast<int*>(&sT[idx[k]]), __float_as_int(nw[k]));
+          else T[k] = nw[k];
+        }
+      }
+      __syncthreads();
+      if (act) {
+#pragma unroll
+        for (int k = 0; k < D1; ++k)
+          if (idx[k] < nvp) T[k] = sT[idx[k]];
+      }
+      __syncthreads();
+    }
+    int con = 1;
+    for (int i = tid; i < nvp; i += blockDim.x) {
+      const int v = vs + i;
+      const float nt = sT[i];
+      float outv;
+      if (!s.seed[v]) {
+        if (!CHECK) s.DT_out[v] = nt;
+        con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
+        outv = nt;
+      } else {
+        outv = s.DT[v];
+      }
+      if (!CHECK) atomicMin(&s_min, __float_as_uint(outv));
+    }
+    if (D1 == 4 && sp.tau > 0.f) {
+      nflag = __reduce_add_sync(0xffffffffu, nflag);
+      if ((tid & 31) == 0 && nflag) atomicAdd(&s.stats[6], (unsigned long long)nflag);
+    }
+    con = __syncthreads_and(con);
+    if (tid == 0) {
+      if (!CHECK) {
+        atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
+        s.bcon[p] = con;
+        s.bmin[p] = __uint_as_float(s_min);
+        s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
+      } else {
+        if (!con) {
+          const int pos = atomicAdd(&s.counts[nxt], 1);
+          nlist[pos] = p;
+        } else {
+          s.blabel[p] = LS_FAR;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Schedule of one FIM iteration: one warp per patch of the current list.
+__global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
+  const int count = s.counts[cur];
+  const int* list = cur ? s.list1 : s.list0;
+  int* nlist = cur ? s.list0 : s.list1;
+  const int nxt = cur ^ 1;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int w = warp_id_global(); w < count; w += nwarps) {
+    const int p = list[w];
+    const int vs = m.vert_off[p], ve = m.vert_off[p + 1];
+    for (int v = vs + lane; v < ve; v += 32)
+      if (!s.seed[v]) s.DT[v] = s.DT_out[v];
+    const int con = s.bcon[p];
+    if (!con) {
+      if (lane == 0) {
+        const int pos = atomicAdd(&s.counts[nxt], 1);
+        nlist[pos] = p;
+      }
+    } else if (s.bmin[p] < sp.bandwidth) {
+      const int a = m.padj_off[p], b = m.padj_off[p + 1];
+      for (int j0 = a; j0 < b; j0 += 32) {
+        const int j = j0 + lane;
+        int q = -1;
+        bool take = false;
+        if (j < b) {
+          q = m.padj[j];
+          take = atomicCAS(&s.blabel[q], LS_FAR, LS_ACTIVE) == LS_FAR;
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, take);
+        if (mask) {
+          const int leader = __ffs(mask) - 1;
+          int base = 0;
+          if (lane == leader) base = atomicAdd(&s.counts[2], __popc(mask));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (take) s.newlist[base + __popc(mask & ((1u << lane) - 1u))] = q;
+        }
+      }
+    }
+  }
+}
+
+// Narrowband (K14) fused with the sign recovery (K10b) and the vertex-update
+// count: one warp per patch over every patch.
+__global__ void k_narrowband(DevMesh m, DevState s, StepParams sp) {
+  __shared__ unsigned long long s_cnt, s_pv, s_np;
+  if (threadIdx.x == 0) { s_cnt = 0; s_pv = 0; s_np = 0; }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  unsigned cnt = 0, pv = 0, npc = 0;
+  for (int p = warp_id_global(); p < m.nparts; p += nwarps) {
+    const int vs = m.vert_off[p], ve = m.vert_off[p + 1];
+    unsigned mn = 0x7f800000u;
+    for (int v = vs + lane; v < ve; v += 32) {
+      const float d = s.DT[v];
+      mn = min(mn, __float_as_uint(d));
+      cnt += (d <= sp.bandwidth);
+      const float mag = (d >= sp.largenum || sp.scale == 1.f) ? d : d * sp.scale;
+      s.phi[v] = s.sign[v] ? mag : -mag;
+    }
+    mn = __reduce_min_sync(0xffffffffu, mn);
+    if (lane == 0 && __uint_as_float(mn) <= sp.bandwidth) {
+      const int pos = atomicAdd(&s.counts[3], 1);
+      s.nblist[pos] = p;
+      pv += ve - vs;
+      npc += 1;
+    }
+  }
+  atomicAdd(&s_cnt, (unsigned long long)cnt);
+  if (lane == 0) { atomicAdd(&s_pv, (unsigned long long)pv); atomicAdd(&s_np, (unsigned long long)npc); }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&s.stats[2], s_cnt);
+    atomicAdd(&s.stats[3], s_pv);
+    atomicAdd(&s.stats[4], s_np);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Update on narrowband patches: advection (meshFIM_kernels.h:36-408,
+// meshFIM2d_kernels.h:37-362) or mean curvature (meshFIM3d.cu:103-267 in the
+// reference form, or the lumped-mass form).  One CTA per patch; per-copy
+// contributions go to shared memory, each owned vertex sums its slots in the
+// reference order.
+struct Contrib {
+  float aH[4], aV[4], curv[4], vol, g0, g1, g2;
+};
+
+template <int D1>
+__device__ __forceinline__ void update_copy(const DevMesh& m, const StepParams& sp, long long c,
+                                            long long c_first, const float* sPhi, const float* sX,
+                                            int nslab, const int idx[4], Contrib& o) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { o.aH[k] = 0.f; o.aV[k] = 0.f; o.curv[k] = 0.f; }
+  o.vol = 0.f; o.g0 = 0.f; o.g1 = 0.f; o.g2 = 0.f;
+  const bool curvature = sp.update_kind == 1;
+  float e[4];
+#pragma unroll
+  for (int k = 0; k < D1; ++k) e[k] = sPhi[idx[k]];
+  if (D1 == 4) {
+    float x[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      x[k][0] = sX[idx[k]];
+      x[k][1] = sX[nslab + idx[k]];
+      x[k][2] = sX[2 * nslab + idx[k]];
+    }
+    const float v31[3] = {x[1][0] - x[3][0], x[1][1] - x[3][1], x[1][2] - x[3][2]};
+    const float v32[3] = {x[2][0] - x[3][0], x[2][1] - x[3][1], x[2][2] - x[3][2]};
+    const float v30[3] = {x[0][0] - x[3][0], x[0][1] - x[3][1], x[0][2] - x[3][2]};
+    const float cr0 = v31[1] * v32[2] - v31[2] * v32[1];
+    const float cr1 = v31[2] * v32[0] - v31[0] * v32[2];
+    const float cr2 = v31[0] * v32[1] - v31[1] * v32[0];
+    const float volume = fabsf(cr0 * v30[0] + cr1 * v30[1] + cr2 * v30[2]) / 6.0f;
+    // gradients of the linear shape functions: rows of the inverse of
+    // [[x0 y0 z0 1]; ...; [x3 y3 z3 1]] by cofactors (meshFIM_kernels.h:173-215)
+    const float a11 = x[0][0], a12 = x[0][1], a13 = x[0][2];
+    const float a21 = x[1][0], a22 = x[1][1], a23 = x[1][2];
+    const float a31 = x[2][0], a32 = x[2][1], a33 = x[2][2];
+    const float a41 = x[3][0], a42 = x[3][1], a43 = x[3][2];
+    const float det =
+        a11 * a22 * a33 + a11 * a23 * a42 + a11 * a32 * a43 + a12 * a21 * a43 + a12 * a23 * a31 +
+        a12 * a33 * a41 + a13 * a21 * a32 + a13 * a22 * a41 + a13 * a31 * a42 + a21 * a33 * a42 +
+        a22 * a31 * a43 + a23 * a32 * a41 - a11 * a22 * a43 - a11 * a23 * a32 - a11 * a33 * a42 -
+        a12 * a21 * a33 - a12 * a23 * a41 - a12 * a31 * a43 - a13 * a21 * a42 - a13 * a22 * a31 -
+        a13 * a32 * a41 - a21 * a32 * a43 - a22 * a33 * a41 - a23 * a31 * a42;
+    const float b11 = a22 * a33 + a23 * a42 + a32 * a43 - a22 * a43 - a23 * a32 - a33 * a42;
+    const float b12 = a12 * a43 + a13 * a32 + a33 * a42 - a12 * a33 - a13 * a42 - a32 * a43;
+    const float b13 = a12 * a23 + a13 * a42 + a22 * a43 - a12 * a43 - a13 * a22 - a23 * a42;
+    const float b14 = a12 * a33 + a13 * a22 + a23 * a32 - a12 * a23 - a13 * a32 - a22 * a33;
+    const float b21 = a21 * a43 + a23 * a31 + a33 * a41 - a21 * a33 - a23 * a41 - a31 * a43;
+    const float b22 = a11 * a33 + a13 * a41 + a31 * a43 - a11 * a43 - a13 * a31 - a33 * a41;
+    const float b23 = a11 * a43 + a13 * a21 + a23 * a41 - a11 * a23 - a13 * a41 - a21 * a43;
+    const float b24 = a11 * a23 + a13 * a31 + a21 * a33 - a11 * a33 - a13 * a21 - a23 * a31;
+    const float b31 = a21 * a32 + a22 * a41 + a31 * a42 - a21 * a42 - a22 * a31 - a32 * a41;
+    const float b32 = a11 * a42 + a12 * a31 + a32 * a41 - a11 * a32 - a12 * a41 - a31 * a42;
+    const float b33 = a11 * a22 + a12 * a41 + a21 * a42 - a11 * a42 - a12 * a21 - a22 * a41;
+    const float b34 = a11 * a32 + a12 * a21 + a22 * a31 - a11 * a22 - a12 * a31 - a21 * a32;
+    float nN[4][3] = {{b11 / det, b21 / det, b31 / det},
+                      {b12 / det, b22 / det, b32 / det},
+                      {b13 / det, b23 / det, b33 / det},
+                      {b14 / det, b24 / det, b34 / det}};
+    float gp0 = 0.f, gp1 = 0.f, gp2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      gp0 += nN[i][0] * e[i];
+      gp1 += nN[i][1] * e[i];
+      gp2 += nN[i][2] * e[i];
+    }
+    const float absg = sqrtf(gp0 * gp0 + gp1 * gp1 + gp2 * gp2);
+    float sg0, sg1, sg2;
+    if (curvature) {
+      sg0 = 1.f; sg1 = 0.f; sg2 = 1.f;
+    } else {
+      const long long cs = sp.ref_compat ? c_first : c;
+      sg0 = __ldg(m.sig + cs); sg1 = __ldg(m.sig + m.full + cs); sg2 = __ldg(m.sig + 2 * m.full + cs);
+    }
+    float K[4], Kp[4], Km[4], H = 0.f, beta = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      K[i] = volume * (sg0 * nN[i][0] + sg1 * nN[i][1] + sg2 * nN[i][2]);
+      H += K[i] * e[i];
+      Kp[i] = fmaxf(K[i], 0.f);
+      Km[i] = fminf(K[i], 0.f);
+      beta += Km[i];
+    }
+    beta = 1.0f / beta;
+    const bool hpass = (double)fabsf(H) > (curvature ? 1e-16 : 1e-8);
+    float at[4] = {0.f, 0.f, 0.f, 0.f};
+    if (hpass) {
+      float alpha[4], theta = 0.f;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float d = Kp[i] * beta *
+                        (Km[0] * (e[i] - e[0]) + Km[1] * (e[i] - e[1]) + Km[2] * (e[i] - e[2]) + Km[3] * (e[i] - e[3]));
+        alpha[i] = d / H;
+        theta += fmaxf(0.f, alpha[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) at[i] = fmaxf(alpha[i], 0.f) / theta;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { o.aH[i] = at[i] * H; o.aV[i] = at[i] * volume; }
+    if (curvature) {
+      const bool gate = sp.ref_compat ? hpass : (absg > 0.f);
+      if (gate) {
+        o.vol = volume;
+        o.g0 = volume * gp0; o.g1 = volume * gp1; o.g2 = volume * gp2;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          float acc = 0.f;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int jj = (i + j) & 3;
+            acc += (nN[i][0] * nN[jj][0] + nN[i][1] * nN[jj][1] + nN[i][2] * nN[jj][2]) / absg * e[jj];
+          }
+          o.curv[i] = volume * acc;
+        }
+      }
+    }
+  } else {
+    const float lc0 = __ldg(m.lc + c), lc1 = __ldg(m.lc + m.full + c), lc2 = __ldg(m.lc + 2 * m.full + c);
+    const float z = lc0 * lc2;  // (AB x AC).z in the local frame
+    const float volume = sqrtf(z * z) / 2.0f;
+    const float det = lc0 * lc2;
+    const float nN[3][2] = {{-lc2 / det, (lc1 - lc0) / det}, {lc2 / det, -lc1 / det}, {0.f / det, lc0 / det}};
+    float gp0 = 0.f, gp1 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { gp0 += nN[i][0] * e[i]; gp1 += nN[i][1] * e[i]; }
+    const float absg = sqrtf(gp0 * gp0 + gp1 * gp1);
+    if (!curvature) {
+      float sg0, sg1;
+      if (sp.ref_compat) {  // meshFIM2d_kernels.h:178-181
+        sg0 = e[0] / absg;
+        sg1 = e[1] / absg;
+      } else {
+        sg0 = __ldg(m.sig + c);
+        sg1 = __ldg(m.sig + m.full + c);
+      }
+      float K[3], Kp[3], Km[3], H = 0.f, beta = 0.f;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        K[i] = volume * (sg0 * nN[i][0] + sg1 * nN[i][1]);
+        H += K[i] * e[i];
+        Kp[i] = fmaxf(K[i], 0.f);
+        Km[i] = fminf(K[i], 0.f);
+        beta += Km[i];
+      }
+      beta = 1.0f / beta;
+      if ((double)fabsf(H) > 1e-8) {
+        float alpha[3], theta = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float d = Kp[i] * beta * (Km[0] * (e[i] - e[0]) + Km[1] * (e[i] - e[1]) + Km[2] * (e[i] - e[2]));
+          alpha[i] = d / H;
+          theta += fmaxf(0.f, alpha[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float a = fmaxf(alpha[i], 0.f) / theta;
+          o.aH[i] = a * H;
+          o.aV[i] = a * volume;
+        }
+      }
+    } else if (absg > 0.f) {
+      o.vol = volume;
+      o.g0 = volume * gp0; o.g1 = volume * gp1;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        float acc = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int jj = (i + j) % 3;
+          acc += (nN[i][0] * nN[jj][0] + nN[i][1] * nN[jj][1]) / absg * e[jj];
+        }
+        o.curv[i] = volume * acc;
+      }
+    }
+  }
+}
+
+template <int D1>
+__global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParams sp) {
+  extern __shared__ float smem[];
+  const int slab = sp.lvp + sp.lgp;
+  float* sPhi = smem;                // slab
+  float* sX = smem + slab;           // 3 * slab (3D only)
+  float* sC = sX + (D1 == 4 ? 3 * slab : 0);  // per copy: aH[4] aV[4] curv[4] vol g0 g1 g2
+  const bool curvature = sp.update_kind == 1;
+  const int stride = 15;
+  const int count = s.counts[3];
+  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+    const int p = s.nblist[li];
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
+    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+    const int nslab = nvp + ngp;
+    for (int i = threadIdx.x; i < nslab; i += blockDim.x) {
+      const int v = i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp);
+      sPhi[i] = s.phi[v];
+      if (D1 == 4) {
+        sX[i] = __ldg(m.xyz + v);
+        sX[nslab + i] = __ldg(m.xyz + m.nv + v);
+        sX[2 * nslab + i] = __ldg(m.xyz + 2 * (long long)m.nv + v);
+      }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nep; c += blockDim.x) {
+      const ushort4 cv = m.conn[es + c];
+      const int idx[4] = {cv.x, cv.y, cv.z, D1 == 4 ? cv.w : 0};
+      Contrib o;
+      update_copy<D1>(m, sp, (long long)es + c, es, sPhi, sX, nslab, idx, o);
+      float* dst = sC + (size_t)c * stride;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { dst[k] = o.aH[k]; dst[4 + k] = o.aV[k]; dst[8 + k] = o.curv[k]; }
+      dst[12] = o.vol; dst[13] = o.g0; dst[14] = o.g1;
+      // g2 packed separately below the copies
+      sC[(size_t)nep * stride + c] = o.g2;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nvp; i += blockDim.x) {
+      const int v = vs + i;
+      const int a = m.vslot_off[v], b = m.vslot_off[v + 1];
+      const float oldT = sPhi[i];
+      float res = oldT;
+      if (!curvature) {
+        float up = 0.f, down = 0.f;
+        for (int q = a; q < b; ++q) {
+          const int sl = m.vslot[q];
+          up += sC[(sl >> 2) * stride + (sl & 3)];
+        }
+        for (int q = a; q < b; ++q) {
+          const int sl = m.vslot[q];
+          down += sC[(sl >> 2) * stride + 4 + (sl & 3)];
+        }
+        if ((double)fabsf(down) > 1e-8) res = oldT - sp.dt * (up / down);
+      } else {
+        float down = 0.f, gd = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, cu = 0.f;
+        for (int q = a; q < b; ++q) {
+          const int sl = m.vslot[q];
+          const float* src = sC + (sl >> 2) * stride;
+          down += src[4 + (sl & 3)];
+          g0 += src[13];
+          g1 += src[14];
+          g2 += sC[(size_t)nep * stride + (sl >> 2)];
+          gd += src[12];
+          cu += src[8 + (sl & 3)];
+        }
+        const float node_eik = sqrtf(g0 * g0 + g1 * g1 + g2 * g2) / gd;
+        if (sp.ref_compat && D1 == 4) {
+          if ((double)fabsf(down) > 1e-16) res = oldT - sp.curv_coeff * node_eik * (cu / gd) * sp.dt;
+        } else if (gd > 0.f) {
+          const float mass = gd / (float)D1;
+          res = oldT - sp.curv_coeff * node_eik * (cu / mass) * sp.dt;
+        }
+      }
+      s.phi_out[v] = res;
+    }
+    __syncthreads();
+  }
+}
+
+// phi := phi_out on narrowband patches (CopyOutBack_levelset3d)
+__global__ void k_copy_phi(DevMesh m, DevState s) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int count = s.counts[3];
+  for (int w = warp_id_global(); w < count; w += nwarps) {
+    const int p = s.nblist[w];
+    for (int v = m.vert_off[p] + lane; v < m.vert_off[p + 1]; v += 32) s.phi[v] = s.phi_out[v];
+  }
+}
+
+// out[old] = phi[new] (kernel_compute_vertT_before_permute3d), as a gather
+__global__ void k_unpermute(DevMesh m, const float* phi, float* out) {
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < m.nv; o += gridDim.x * blockDim.x)
+    out[o] = phi[__ldg(m.ipermute + o)];
+}
+
+// out[new] = in[old]
+__global__ void k_permute(DevMesh m, const float* in, float* out) {
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < m.nv; o += gridDim.x * blockDim.x)
+    out[__ldg(m.ipermute + o)] = in[o];
+}
+
+// ---------------------------------------------------------------------------
+// Launchers (host side).
+cudaError_t launch_reset(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st) {
+  k_reset<<<L.flat_grid, 256, 0, st>>>(s, m.nv, sp.largenum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float scale, const Launch& L, cudaStream_t st) {
+  if (m.dim == 3) k_seed<4><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, use_all, scale);
+  else k_seed<3><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, use_all, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
+                         const Launch& L, cudaStream_t st) {
+  const bool big = L.fim_block > 512;
+  const bool xd = sp.xdiv != 0;
+  const int c = check ? 1 : 0;
+#define LS_FIM(D, T, X) k_fim<D, T, X><<<L.fim_grid, L.fim_block, L.fim_smem, st>>>(m, s, sp, cur, c)
+  if (m.dim == 3) {
+    if (big) { if (xd) LS_FIM(4, 1024, true); else LS_FIM(4, 1024, false); }
+    else { if (xd) LS_FIM(4, 512, true); else LS_FIM(4, 512, false); }
+  } else {
+    if (big) LS_FIM(3, 1024, false); else LS_FIM(3, 512, false);
+  }
+#undef LS_FIM
+  return cudaGetLastError();
+}
+
+cudaError_t launch_schedule(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, const Launch& L,
+                            cudaStream_t st) {
+  k_schedule<<<L.warp_grid, 256, 0, st>>>(m, s, sp, cur);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_narrowband(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                              cudaStream_t st) {
+  k_narrowband<<<L.warp_grid, 256, 0, st>>>(m, s, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                          cudaStream_t st) {
+  if (m.dim == 3) k_update<4><<<L.upd_grid, L.upd_block, L.upd_smem, st>>>(m, s, sp);
+  else k_update<3><<<L.upd_grid, L.upd_block, L.upd_smem, st>>>(m, s, sp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_copy_phi<<<L.warp_grid, 256, 0, st>>>(m, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpermute(const DevMesh& m, const float* phi, float* out, const Launch& L, cudaStream_t st) {
+  k_unpermute<<<L.flat_grid, 256, 0, st>>>(m, phi, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_permute(const DevMesh& m, const float* in, float* out, const Launch& L, cudaStream_t st) {
+  k_permute<<<L.flat_grid, 256, 0, st>>>(m, in, out);
+  return cudaGetLastError();
+}
+
+cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) return e;
+  L.sms = prop.multiProcessorCount;
+  L.fim_block = ((sp.lep + 31) / 32) * 32;
+  if (L.fim_block < 64) L.fim_block = 64;
+  L.fim_smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
+  int occ = 0;
+  if (m.dim == 3) {
+    if (L.fim_block > 512)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 1024, false>, L.fim_block, L.fim_smem);
+    else
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 512, false>, L.fim_block, L.fim_smem);
+  } else {
+    if (L.fim_block > 512)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 1024, false>, L.fim_block, L.fim_smem);
+    else
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 512, false>, L.fim_block, L.fim_smem);
+  }
+  if (e != cudaSuccess) return e;
+  if (occ < 1) occ = 1;
+  L.fim_grid = L.sms * occ;
+  L.seed_grid = L.sms * 8;
+  L.upd_block = L.fim_block > 512 ? 512 : L.fim_block;
+  const int slab = sp.lvp + sp.lgp;
+  L.upd_smem = (int)sizeof(float) * (slab * (m.dim == 3 ? 4 : 1) + sp.lep * 16);
+  if (L.upd_smem > 48 * 1024) {
+    if (m.dim == 3) e = cudaFuncSetAttribute(k_update<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, L.upd_smem);
+    else e = cudaFuncSetAttribute(k_update<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, L.upd_smem);
+    if (e != cudaSuccess) return e;
+  }
+  occ = 0;
+  if (m.dim == 3) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update<4>, L.upd_block, L.upd_smem);
+  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update<3>, L.upd_block, L.upd_smem);
+  if (e != cudaSuccess) return e;
+  if (occ < 1) occ = 1;
+  L.upd_grid = L.sms * occ;
+  L.warp_grid = L.sms * 8;
+  L.flat_grid = L.sms * 8;
+  return cudaSuccess;
+}
+
+
+const KernelSet& kernel_table() {
+  static const KernelSet t = {configure_launch, launch_reset, launch_seed, launch_sweep, launch_schedule,
+                              launch_narrowband, launch_update, launch_unpermute, launch_permute};
+  return t;
+}

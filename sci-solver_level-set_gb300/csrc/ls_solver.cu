@@ -63,6 +63,7 @@ std::string Solver::check(cudaError_t e, const char* what) {
 std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* vel) {
   lay_ = &L;
   cfg_ = cfg;
+  K_ = cfg.bit_exact ? &kernels_exact() : &kernels_fast();
   if (L.lep > 1024) { status_ = 2; return "a patch has more than 1024 element copies"; }
   LS_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   LS_TRY(cudaEventCreate(&ev0_), "event");
@@ -162,6 +163,7 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   sp_.bandwidth = (float)(cfg.bandwidth / scale);
   sp_.scale = (float)scale;
   sp_.tau = (cfg.fp64_flagged && L.dim == 3) ? (float)cfg.fp64_tau : 0.f;
+  sp_.xdiv = (cfg.bit_exact && ref) ? 1 : 0;
   sp_.tol = (float)cfg.smallnum;
   sp_.eps_h64 = cfg.smallnum;
   sp_.eps_h = (float)sp_.eps_h64;
@@ -174,7 +176,7 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   sp_.lgp = L.lgp;
   sp_.lep = L.lep;
   (void)d1;
-  LS_TRY(configure_launch(m_, sp_, L_), "configure");
+  LS_TRY(K_->configure(m_, sp_, L_), "configure");
   if (cfg_.graph_chunk < 2) cfg_.graph_chunk = 2;
   if (cfg_.graph_chunk & 1) cfg_.graph_chunk++;
   if (cfg_.use_graph) {
@@ -190,9 +192,9 @@ std::string Solver::build_graph() {
   cudaError_t err = cudaSuccess;
   for (int i = 0; i < cfg_.graph_chunk && err == cudaSuccess; ++i) {
     const int cur = i & 1;
-    err = launch_sweep(m_, s_, sp_, cur, false, L_, stream_);
-    if (err == cudaSuccess) err = launch_schedule(m_, s_, sp_, cur, L_, stream_);
-    if (err == cudaSuccess) err = launch_sweep(m_, s_, sp_, cur, true, L_, stream_);
+    err = K_->sweep(m_, s_, sp_, cur, false, L_, stream_);
+    if (err == cudaSuccess) err = K_->schedule(m_, s_, sp_, cur, L_, stream_);
+    if (err == cudaSuccess) err = K_->sweep(m_, s_, sp_, cur, true, L_, stream_);
   }
   cudaError_t e2 = cudaStreamEndCapture(stream_, &graph_);
   LS_TRY(err, "capture launch");
@@ -234,9 +236,9 @@ std::string Solver::fim_loop() {
     } else {
       for (int i = 0; i < cfg_.graph_chunk; ++i) {
         const int cur = i & 1;
-        LS_TRY(prof(0, [&] { return launch_sweep(m_, s_, sp_, cur, false, L_, stream_); }), "sweep");
-        LS_TRY(prof(2, [&] { return launch_schedule(m_, s_, sp_, cur, L_, stream_); }), "schedule");
-        LS_TRY(prof(1, [&] { return launch_sweep(m_, s_, sp_, cur, true, L_, stream_); }), "check");
+        LS_TRY(prof(0, [&] { return K_->sweep(m_, s_, sp_, cur, false, L_, stream_); }), "sweep");
+        LS_TRY(prof(2, [&] { return K_->schedule(m_, s_, sp_, cur, L_, stream_); }), "schedule");
+        LS_TRY(prof(1, [&] { return K_->sweep(m_, s_, sp_, cur, true, L_, stream_); }), "check");
       }
     }
     launched += cfg_.graph_chunk;
@@ -269,14 +271,14 @@ std::string Solver::one_step(bool* empty_nb) {
   const int use_all = have_nb_ ? 0 : 1;
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_), "memset");
-  LS_TRY(launch_reset(m_, s_, sp_, L_, stream_), "reset");
+  LS_TRY(K_->reset(m_, s_, sp_, L_, stream_), "reset");
   LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_), "memset");
-  LS_TRY(prof(3, [&] { return launch_seed(m_, s_, use_all, sp_.scale, L_, stream_); }), "seed");
+  LS_TRY(prof(3, [&] { return K_->seed(m_, s_, use_all, sp_.scale, L_, stream_); }), "seed");
   LS_TRY(cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_), "memset");
   st_.kernel_launches += 3;  // reset, seed, narrowband
   std::string r = fim_loop();
   if (!r.empty()) return r;
-  LS_TRY(prof(4, [&] { return launch_narrowband(m_, s_, sp_, L_, stream_); }), "narrowband");
+  LS_TRY(prof(4, [&] { return K_->narrowband(m_, s_, sp_, L_, stream_); }), "narrowband");
   LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
   LS_TRY(cudaStreamSynchronize(stream_), "nb sync");
   if (h_counts_[3] == 0) {
@@ -287,7 +289,7 @@ std::string Solver::one_step(bool* empty_nb) {
   have_nb_ = true;
   if (cfg_.update_kind != 2) {
     for (int it = 0; it < cfg_.inside_niter; ++it) {
-      LS_TRY(prof(5, [&] { return launch_update(m_, s_, sp_, L_, stream_); }), "update");
+      LS_TRY(prof(5, [&] { return K_->update(m_, s_, sp_, L_, stream_); }), "update");
       st_.kernel_launches += 2;  // update, copy-back
     }
   }
@@ -325,7 +327,7 @@ void Solver::pull_stats() {
 std::string Solver::run(int nsteps, float* history, int* steps_done) {
   int done = 0;
   if (history) {
-    LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+    LS_TRY(K_->unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
     LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
     LS_TRY(cudaStreamSynchronize(stream_), "sync");
     std::memcpy(history, h_stage_, sizeof(float) * m_.nv);
@@ -338,7 +340,7 @@ std::string Solver::run(int nsteps, float* history, int* steps_done) {
     if (empty) break;
     done++;
     if (history) {
-      LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+      LS_TRY(K_->unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
       LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
       LS_TRY(cudaStreamSynchronize(stream_), "sync");
       std::memcpy(history + (size_t)(s + 1) * m_.nv, h_stage_, sizeof(float) * m_.nv);
@@ -358,30 +360,31 @@ std::string Solver::run(int nsteps, float* history, int* steps_done) {
 std::string Solver::step_host(const float* phi_in, float* phi_out) {
   std::memcpy(h_stage_, phi_in, sizeof(float) * m_.nv);
   LS_TRY(cudaMemcpyAsync(d_tmp_, h_stage_, sizeof(float) * m_.nv, cudaMemcpyHostToDevice, stream_), "h2d");
-  LS_TRY(launch_permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
+  LS_TRY(K_->permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
   st_.kernel_launches += 2;  // permute in, unpermute out
   bool empty = false;
   std::string r = one_step(&empty);
   if (!r.empty()) return r;
-  LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+  LS_TRY(K_->unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
   LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   std::memcpy(phi_out, h_stage_, sizeof(float) * m_.nv);
   if (!empty) st_.steps_run++;
+  pull_stats();
   return "";
 }
 
 std::string Solver::set_phi(const float* phi_orig) {
   std::memcpy(h_stage_, phi_orig, sizeof(float) * m_.nv);
   LS_TRY(cudaMemcpyAsync(d_tmp_, h_stage_, sizeof(float) * m_.nv, cudaMemcpyHostToDevice, stream_), "h2d");
-  LS_TRY(launch_permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
+  LS_TRY(K_->permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   have_nb_ = false;
   return "";
 }
 
 std::string Solver::get_phi(float* phi_orig) {
-  LS_TRY(launch_unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
+  LS_TRY(K_->unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
   LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost, stream_), "d2h");
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   std::memcpy(phi_orig, h_stage_, sizeof(float) * m_.nv);

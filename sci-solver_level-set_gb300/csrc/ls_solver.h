@@ -20,24 +20,29 @@ struct Launch {
   int flat_grid;
 };
 
-cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L);
-cudaError_t launch_reset(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st);
-cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float scale, const Launch& L, cudaStream_t st);
-cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
-                         const Launch& L, cudaStream_t st);
-cudaError_t launch_schedule(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, const Launch& L,
-                            cudaStream_t st);
-cudaError_t launch_narrowband(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
-                              cudaStream_t st);
-cudaError_t launch_update(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+// One build of the step kernels (fast or bit-exact).
+struct KernelSet {
+  cudaError_t (*configure)(const DevMesh& m, const StepParams& sp, Launch& L);
+  cudaError_t (*reset)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st);
+  cudaError_t (*seed)(const DevMesh& m, const DevState& s, int use_all, float scale, const Launch& L, cudaStream_t st);
+  cudaError_t (*sweep)(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
+                       const Launch& L, cudaStream_t st);
+  cudaError_t (*schedule)(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, const Launch& L,
                           cudaStream_t st);
-cudaError_t launch_unpermute(const DevMesh& m, const float* phi, float* out, const Launch& L, cudaStream_t st);
-cudaError_t launch_permute(const DevMesh& m, const float* in, float* out, const Launch& L, cudaStream_t st);
+  cudaError_t (*narrowband)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                            cudaStream_t st);
+  cudaError_t (*update)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st);
+  cudaError_t (*unpermute)(const DevMesh& m, const float* phi, float* out, const Launch& L, cudaStream_t st);
+  cudaError_t (*permute)(const DevMesh& m, const float* in, float* out, const Launch& L, cudaStream_t st);
+};
+const KernelSet& kernels_fast();
+const KernelSet& kernels_exact();
 
 struct SolverConfig {
   int update_kind = 0;
   int ref_compat = 0;
   int fp64_flagged = 0;
+  int bit_exact = 0;
   int profile = 0;
   int use_graph = 1;
   int niter = 0;
@@ -89,6 +94,7 @@ class Solver {
   void pull_stats();
 
   const Layout* lay_ = nullptr;
+  const KernelSet* K_ = nullptr;
   SolverConfig cfg_;
   DevMesh m_{};
   DevState s_{};
