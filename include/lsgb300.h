@@ -159,6 +159,10 @@ ls_status ls_reset_stats(ls_handle* h);
 ls_status ls_set_profile(ls_handle* h, int on);
 /* Narrowband of the last step: one byte per patch. */
 ls_status ls_get_narrowband(ls_handle* h, unsigned char* flags);
+/* Diagnostics: the current FIM active list (patch ids, at most cap) and,
+ * if dt is given, the FIM distance values in the layout's vertex order
+ * (nv floats, FIM frame units). */
+ls_status ls_debug_active(ls_handle* h, int* list, int cap, int* count, float* dt);
 /* info[0..9] = nparts, full, lep, lvp, lgp, lim, nadj, nv, ne, dim */
 ls_status ls_get_layout_info(ls_handle* h, long long* info);
 /* Reference-format layout arrays (LS_REF_* below) for bit-exact checks. */

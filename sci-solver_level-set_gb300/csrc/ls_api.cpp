@@ -363,6 +363,19 @@ ls_status ls_get_narrowband(ls_handle* h, unsigned char* flags) {
   return solver_status(h, h->solver->narrowband(flags));
 }
 
+ls_status ls_debug_active(ls_handle* h, int* list, int cap, int* count, float* dt) {
+  if (!h || !count) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  std::vector<int> v;
+  std::string r = h->solver->active_patches(v);
+  if (!r.empty()) return solver_status(h, r);
+  *count = (int)v.size();
+  if (list)
+    for (int i = 0; i < (int)v.size() && i < cap; ++i) list[i] = v[i];
+  if (dt) return solver_status(h, h->solver->dt_values(dt));
+  return LS_OK;
+}
+
 ls_status ls_get_layout_info(ls_handle* h, long long* info) {
   if (!h || !info) return LS_BAD_INPUT;
   if (!h->layout) return fail(h, LS_NOT_READY, "call ls_setup first");

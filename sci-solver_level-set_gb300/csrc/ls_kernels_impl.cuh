@@ -383,6 +383,18 @@ __device__ __forceinline__ void update_copy(const DevMesh& m, const StepParams& 
       x[k][1] = sX[nslab + idx[k]];
       x[k][2] = sX[2 * nslab + idx[k]];
     }
+    if (!sp.ref_compat) {
+      // shape-function gradients from coordinates relative to the fourth
+      // vertex (translation invariant, well conditioned in FP32); the
+      // reference's absolute-coordinate cofactors cancel to O(h^3)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        x[k][0] = x[k][0] - x[3][0];
+        x[k][1] = x[k][1] - x[3][1];
+        x[k][2] = x[k][2] - x[3][2];
+      }
+      x[3][0] = 0.f; x[3][1] = 0.f; x[3][2] = 0.f;
+    }
     const float v31[3] = {x[1][0] - x[3][0], x[1][1] - x[3][1], x[1][2] - x[3][2]};
     const float v32[3] = {x[2][0] - x[3][0], x[2][1] - x[3][1], x[2][2] - x[3][2]};
     const float v30[3] = {x[0][0] - x[3][0], x[0][1] - x[3][1], x[0][2] - x[3][2]};
@@ -608,8 +620,8 @@ __global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParam
         if (sp.ref_compat && D1 == 4) {
           if ((double)fabsf(down) > 1e-16) res = oldT - sp.curv_coeff * node_eik * (cu / gd) * sp.dt;
         } else if (gd > 0.f) {
-          const float mass = gd / (float)D1;
-          res = oldT - sp.curv_coeff * node_eik * (cu / mass) * sp.dt;
+          // the reference's normalisation (curv_up / sum of element volumes)
+          res = oldT - sp.curv_coeff * node_eik * (cu / gd) * sp.dt;
         }
       }
       s.phi_out[v] = res;

@@ -402,6 +402,20 @@ std::string Solver::narrowband(unsigned char* flags) {
   return "";
 }
 
+std::string Solver::active_patches(std::vector<int>& out) {
+  LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  out.assign(h_counts_[0], 0);
+  if (h_counts_[0] > 0) LS_TRY(cudaMemcpy(out.data(), s_.list0, sizeof(int) * h_counts_[0], cudaMemcpyDeviceToHost), "d2h");
+  return "";
+}
+
+std::string Solver::dt_values(float* dt) {
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  LS_TRY(cudaMemcpy(dt, s_.DT, sizeof(float) * m_.nv, cudaMemcpyDeviceToHost), "d2h");
+  return "";
+}
+
 void Solver::stats(SolverStats& s) const { s = st_; }
 
 void Solver::reset_stats() {

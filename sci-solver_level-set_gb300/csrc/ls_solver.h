@@ -81,6 +81,8 @@ class Solver {
   std::string run(int nsteps, float* history, int* steps_done);
   std::string step_host(const float* phi_in, float* phi_out);
   std::string narrowband(unsigned char* flags);
+  std::string active_patches(std::vector<int>& out);
+  std::string dt_values(float* dt_new_order);
   void stats(SolverStats& s) const;
   void reset_stats();
   int status_code() const { return status_; }

@@ -60,7 +60,7 @@ EXPORTS = [
     "ls_set_partition", "ls_set_phi", "ls_set_velocity", "ls_prepare", "ls_setup", "ls_solve", "ls_step",
     "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_narrowband",
     "ls_get_layout_info", "ls_get_layout", "ls_last_error", "ls_version", "ls_partition_structured",
-    "ls_partition_rcb", "ls_set_profile",
+    "ls_partition_rcb", "ls_set_profile", "ls_debug_active",
 ]
 
 _lib = None
@@ -93,6 +93,7 @@ def lib():
     L.ls_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
     L.ls_reset_stats.argtypes = [P]
     L.ls_set_profile.argtypes = [P, I]
+    L.ls_debug_active.argtypes = [P, V, I, ctypes.POINTER(I), V]
     L.ls_get_narrowband.argtypes = [P, V]
     L.ls_get_layout_info.argtypes = [P, V]
     L.ls_get_layout.argtypes = [P, I, V]
@@ -241,6 +242,15 @@ class LevelSet:
         out = np.zeros(nparts, np.uint8)
         self._check(lib().ls_get_narrowband(self._h, _ptr(out)), "get_narrowband")
         return out
+
+    def debug_active(self, with_dt=False):
+        cap = 1 << 20
+        lst = np.zeros(cap, np.int32)
+        n = ctypes.c_int(0)
+        dt = np.zeros(self.nv, np.float32) if with_dt else None
+        self._check(lib().ls_debug_active(self._h, _ptr(lst), cap, ctypes.byref(n),
+                                          _ptr(dt) if dt is not None else None), "debug_active")
+        return lst[: n.value].copy(), dt
 
     def layout_info(self):
         info = np.zeros(10, np.int64)

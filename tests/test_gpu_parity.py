@@ -89,23 +89,24 @@ def test_fast_build_matches_oracle(name, n):
     assert abs(st["nb_vertex_updates"] - ost["nb_vertex_updates"]) <= 0.005 * ost["nb_vertex_updates"]
 
 
-@pytest.mark.parametrize("fp64", [False, True])
-def test_redistance_tracks_fp64_oracle(fp64):
-    # the metric's accuracy bar, max |phi - phi_FP64| <= 1e-3 h, on the
-    # redistance (the curvature update amplifies rounding where
-    # |grad phi| -> 0, see the module docstring)
+@pytest.mark.parametrize("update", ["none", "curvature"])
+def test_precision_form_meets_fp64_bar(update):
+    # the metric's accuracy bar, max |phi - phi_FP64| <= 1e-3 h, met by the
+    # precision form; plain FP32 keeps >= 99% of the band within it
     w = synth.workload("c3", n=24)
-    w["update"] = "none"
-    ls = lsgb300.from_workload(w, fp64_flagged=fp64)
-    hist, _ = ls.solve(1)
-    ref, _, _, _ = _oracle(w, False, 0.0, 1, precision=64)
-    e, band = _band_err(hist[1], ref[1], w)
-    if fp64:
-        assert e.max() <= 1e-3, e.max()
-    else:
-        # plain FP32: cancelled face discriminants leave a few percent of the
-        # band off by more than 1e-3 h (the precision form removes them)
-        assert np.mean(e <= 1e-3) >= 0.98, (np.mean(e <= 1e-3), e.max())
+    w["update"] = update
+    nsteps = 3
+    ref, _, _, _ = _oracle(w, False, 0.0, nsteps, precision=64)
+    prec = lsgb300.from_workload(w, fp64_flagged=True)
+    hp, _ = prec.solve(nsteps)
+    plain = lsgb300.from_workload(w)
+    hf, _ = plain.solve(nsteps)
+    for s in range(1, nsteps + 1):
+        e, _ = _band_err(hp[s], ref[s], w)
+        assert e.max() <= 1e-3, (s, e.max())
+        e, _ = _band_err(hf[s], ref[s], w)
+        assert np.mean(e <= 1e-3) >= 0.98, (s, np.mean(e <= 1e-3), e.max())
+    assert prec.stats()["flagged_copies"] > 0
 
 
 def test_step_host_equals_device_steps():
