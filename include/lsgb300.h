@@ -185,6 +185,32 @@ enum {
   LS_REF_VERT_IPERMUTE = 10        /* int[nv]             vert_ipermute        */
 };
 
+/* Narrowband selection without any device allocation.  No counterpart in
+ * the reference: it is the solver's narrowband kernel (narrowband patches,
+ * phi = +-DT * scale, vertex-update count) for callers that cannot call
+ * cudaMalloc -- host applications that own all device memory through their
+ * own pool, fixed memory budgets, steps recorded once and replayed.  All
+ * pointers except `counts` are device pointers owned by the caller:
+ *   vert_offsets  nparts+1 ints, patch ranges of the vertices (layout order)
+ *   dt            nv floats, FIM distances in the FIM frame
+ *   sign          nv bytes, 1 where phi >= 0 before the redistance
+ *   phi           nv floats, output: +-DT * scale (+-DT where DT >= largenum)
+ *   nb_flags      nparts bytes, output: 1 for narrowband patches
+ *   counts        host, 3 long longs, output: narrowband patches, vertex
+ *                 updates (DT <= bandwidth), vertices of narrowband patches
+ * stream is a cudaStream_t (NULL = default stream); the call synchronises it.
+ * Scratch (the compact patch list and the counters) is a file-scope device
+ * array of LS_NOALLOC_MAX_PATCHES + 64 ints (about 4 MB), held by every GPU
+ * that loads the library until exit; nparts above the limit is rejected
+ * with LS_BAD_INPUT.  The first call on a device looks up the array's device
+ * address (make it before any stream capture).  The array is shared by all
+ * calls and keeps the last call's contents (counters are cleared per call):
+ * calls that overlap on the GPU race. */
+#define LS_NOALLOC_MAX_PATCHES (1 << 20)
+ls_status ls_narrowband_noalloc(int nv, int nparts, const int* vert_offsets, const float* dt,
+                                const unsigned char* sign, float bandwidth, float scale, float largenum,
+                                float* phi, unsigned char* nb_flags, long long* counts, void* stream);
+
 /* Partitioners.  Structured blocks: GraphPartition_Square semantics
  * (meshFIM3d.cu:316-326, meshFIM2d.cu:346-353) on an x-fastest lattice of
  * side nside (3D: nside^3 vertices, 2D: nside^2), block side block. */

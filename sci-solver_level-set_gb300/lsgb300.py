@@ -60,7 +60,7 @@ EXPORTS = [
     "ls_set_partition", "ls_set_phi", "ls_set_velocity", "ls_prepare", "ls_setup", "ls_solve", "ls_step",
     "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_narrowband",
     "ls_get_layout_info", "ls_get_layout", "ls_last_error", "ls_version", "ls_partition_structured",
-    "ls_partition_rcb", "ls_set_profile", "ls_debug_active",
+    "ls_partition_rcb", "ls_set_profile", "ls_debug_active", "ls_narrowband_noalloc",
 ]
 
 _lib = None
@@ -94,6 +94,7 @@ def lib():
     L.ls_reset_stats.argtypes = [P]
     L.ls_set_profile.argtypes = [P, I]
     L.ls_debug_active.argtypes = [P, V, I, ctypes.POINTER(I), V]
+    L.ls_narrowband_noalloc.argtypes = [I, I, V, V, V, ctypes.c_float, ctypes.c_float, ctypes.c_float, V, V, V, V]
     L.ls_get_narrowband.argtypes = [P, V]
     L.ls_get_layout_info.argtypes = [P, V]
     L.ls_get_layout.argtypes = [P, I, V]
