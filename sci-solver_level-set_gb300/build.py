@@ -19,6 +19,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ls_layout.cpp", "ls_api.cpp", "ls_solver.cu", "ls_kernels.cu", "ls_kernels_exact.cu", "ls_noalloc.cu"]
 # translation units compiled without FMA contraction
 NO_FMA = {"ls_kernels_exact.cu"}
+# the fast kernel build: hardware-approximate division and square root
+# (denormals kept); the bit-exact build keeps IEEE-rounded operations
+FAST_DIV_SQRT = {"ls_kernels.cu"}
 
 
 def nvcc():
@@ -47,6 +50,8 @@ def build(verbose=False, ptxas_info=False):
         obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         extra = ["-fmad=false"] if src in NO_FMA else []
+        if src in FAST_DIV_SQRT:
+            extra += ["-prec-div=false", "-prec-sqrt=false"]
         jobs.append([nvcc()] + flags + extra + ["-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(_run, jobs))

@@ -169,8 +169,8 @@ __device__ __forceinline__ void copy_metric(const DevMesh& m, long long c, float
 // differently contracted FMAs could make the check report a drop of more
 // than the tolerance that the following visit never applies, and two
 // patches could re-activate each other without end.
-template <int D1, int MAXT, bool XDIV>
-__global__ void __launch_bounds__(MAXT) k_fim(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+template <int D1, int MAXT, bool XDIV, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepParams sp, int cur, int check) {
   const bool CHECK = check != 0;
   extern __shared__ float smem[];
   float* sT = smem;                       // owned + ghost values
@@ -666,17 +666,21 @@ cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float 
   return cudaGetLastError();
 }
 
+// Block size classes: patches of up to 384 element copies run two CTAs per
+// SM (registers capped at 85), larger ones one CTA of 512 or 1024 threads.
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
                          const Launch& L, cudaStream_t st) {
-  const bool big = L.fim_block > 512;
   const bool xd = sp.xdiv != 0;
   const int c = check ? 1 : 0;
-#define LS_FIM(D, T, X) k_fim<D, T, X><<<L.fim_grid, L.fim_block, L.fim_smem, st>>>(m, s, sp, cur, c)
+#define LS_FIM(D, T, X, B) k_fim<D, T, X, B><<<L.fim_grid, L.fim_block, L.fim_smem, st>>>(m, s, sp, cur, c)
   if (m.dim == 3) {
-    if (big) { if (xd) LS_FIM(4, 1024, true); else LS_FIM(4, 1024, false); }
-    else { if (xd) LS_FIM(4, 512, true); else LS_FIM(4, 512, false); }
+    if (L.fim_block <= 384) { if (xd) LS_FIM(4, 384, true, 2); else LS_FIM(4, 384, false, 2); }
+    else if (L.fim_block <= 512) { if (xd) LS_FIM(4, 512, true, 1); else LS_FIM(4, 512, false, 1); }
+    else { if (xd) LS_FIM(4, 1024, true, 1); else LS_FIM(4, 1024, false, 1); }
   } else {
-    if (big) LS_FIM(3, 1024, false); else LS_FIM(3, 512, false);
+    if (L.fim_block <= 384) LS_FIM(3, 384, false, 2);
+    else if (L.fim_block <= 512) LS_FIM(3, 512, false, 1);
+    else LS_FIM(3, 1024, false, 1);
   }
 #undef LS_FIM
   return cudaGetLastError();
@@ -727,15 +731,19 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   L.fim_smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
   int occ = 0;
   if (m.dim == 3) {
-    if (L.fim_block > 512)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 1024, false>, L.fim_block, L.fim_smem);
+    if (L.fim_block <= 384)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 2>, L.fim_block, L.fim_smem);
+    else if (L.fim_block <= 512)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 512, false, 1>, L.fim_block, L.fim_smem);
     else
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 512, false>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 1024, false, 1>, L.fim_block, L.fim_smem);
   } else {
-    if (L.fim_block > 512)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 1024, false>, L.fim_block, L.fim_smem);
+    if (L.fim_block <= 384)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 384, false, 2>, L.fim_block, L.fim_smem);
+    else if (L.fim_block <= 512)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 512, false, 1>, L.fim_block, L.fim_smem);
     else
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 512, false>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 1024, false, 1>, L.fim_block, L.fim_smem);
   }
   if (e != cudaSuccess) return e;
   if (occ < 1) occ = 1;
