@@ -161,6 +161,7 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="cells per side (128 = the benchmark workload)")
     ap.add_argument("--fp64-flagged", action="store_true", help="precision form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 0 = library default)")
     args = ap.parse_args()
     rank, world, local = env_rank()
 
@@ -182,7 +183,8 @@ def main():
         dist_mod.init_process_group("gloo")
         dist = dist_mod
     torch.cuda.set_device(local)
-    ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged)
+    extra = {"fim_ctas_per_sm": args.ctas} if args.ctas else {}
+    ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged, **extra)
     nv = len(w["xyz"])
     # L2 flush buffer (larger than the 129 MB L2), written between timed steps
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")

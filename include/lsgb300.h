@@ -96,6 +96,7 @@ typedef struct ls_params {
   double length_scale;    /* FIM length unit when not LS_REF_COMPAT (0 -> mean edge length) */
   double fp64_threshold;  /* LS_FP64_FLAGGED: discriminant cancellation threshold tau (0 -> 2^-18) */
   int graph_chunk;        /* FIM iterations per graph launch / host check (0 -> 4) */
+  int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 (0 -> 3) */
 } ls_params;
 
 typedef struct ls_stats {

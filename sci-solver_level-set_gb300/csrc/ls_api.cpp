@@ -99,6 +99,7 @@ ls_status ls_default_params(ls_params* p) {
   p->length_scale = 0.0;
   p->fp64_threshold = 3.814697265625e-06;
   p->graph_chunk = 4;
+  p->fim_ctas_per_sm = 3;
   return LS_OK;
 }
 
@@ -281,6 +282,7 @@ ls_status ls_setup(ls_handle* h) {
   cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
   cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;
   cfg.graph_chunk = p.graph_chunk > 0 ? p.graph_chunk : 4;
+  cfg.fim_ctas = p.fim_ctas_per_sm > 0 ? p.fim_ctas_per_sm : 3;
   cfg.dt = p.time_step;
   cfg.bandwidth = p.bandwidth;
   cfg.curv_coeff = p.curv_coeff;

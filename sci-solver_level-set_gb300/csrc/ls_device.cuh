@@ -62,6 +62,7 @@ struct StepParams {
   float scale;       // FIM frame length unit (1 with the reference's semantics)
   float tau;         // precision form: discriminant cancellation threshold
   int xdiv;          // interior division in double (bit-exact build, reference semantics)
+  int ctas;          // FIM CTAs per SM for patches of up to 384 copies (2, 3 or 4)
   float tol;       // convergence threshold on oldT - newT
   float eps_h;     // denominator offset of the interior tet update
   double eps_h64;
@@ -93,7 +94,7 @@ __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a,
 // `tau` > 0 turns on the conditioning check of the precision form: `ill` is
 // set when a discriminant q^2 - 4pr cancels, |q^2 - 4pr| <= tau (q^2 + |4pr|),
 // i.e. when FP32 has lost about log2(1/tau) bits of it.
-template <typename R, bool XDIV>
+template <typename R, bool XDIV, bool CHK = true>
 __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD, R BCBC, R BCCD,
                                        R CDCD, R eps_h, double eps_h64, R LN, R tau, bool& ill) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
@@ -107,7 +108,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   q = (BCCD + BCCD) * TBC * TBC - two * BCBC * BCCD;
   r = TBC * TBC * CDCD - BCCD * BCCD;
   delta = q * q - four * p * r;
-  ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
     lambda1 = zero;
@@ -135,7 +136,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   r = (TAB * TAB * BCBC - gammay * gammay) + ((BCCD + BCCD) * TAB * TAB - two * gammay * gammaz) +
       (TAB * TAB * CDCD - gammaz * gammaz);
   delta = q * q - four * p * r;
-  ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
 #pragma unroll
@@ -157,7 +158,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   q = (ACCD + ACCD) * TAC * TAC - two * ACAC * ACCD;
   r = TAC * TAC * CDCD - ACCD * ACCD;
   delta = q * q - four * p * r;
-  ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
 #pragma unroll
@@ -183,7 +184,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - two * ACBC * ACCD) * t * h +
       (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
   delta = q * q - four * p * r;
-  ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
 #pragma unroll

@@ -92,7 +92,7 @@ __global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
 // Solves of one element copy (Jacobi: all from the values at sweep start).
 // With the precision form (tau > 0) a solve whose discriminant cancelled is
 // repeated in FP64; `nflag` counts those repeats.
-template <int D1, bool XDIV>
+template <int D1, bool XDIV, bool PREC>
 __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], float out[4], float eps_h,
                                            double eps_h64, float LN, float tau, int& nflag) {
   if (D1 == 4) {
@@ -100,17 +100,17 @@ __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], fl
     const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
     const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
     bool ill[4] = {false, false, false, false};
-    float r3 = tet_solve<float, XDIV>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3]);
-    float r0 = tet_solve<float, XDIV>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0]);
-    float r1 = tet_solve<float, XDIV>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1]);
-    float r2 = tet_solve<float, XDIV>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2]);
-    if (tau > 0.f && (ill[0] | ill[1] | ill[2] | ill[3])) {
+    float r3 = tet_solve<float, XDIV, PREC>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3]);
+    float r0 = tet_solve<float, XDIV, PREC>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0]);
+    float r1 = tet_solve<float, XDIV, PREC>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1]);
+    float r2 = tet_solve<float, XDIV, PREC>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2]);
+    if (PREC && (ill[0] | ill[1] | ill[2] | ill[3])) {
       const double L64 = LN;
       bool d = false;
-      if (ill[3]) { r3 = (float)tet_solve<double, false>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-      if (ill[0]) { r0 = (float)tet_solve<double, false>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-      if (ill[1]) { r1 = (float)tet_solve<double, false>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-      if (ill[2]) { r2 = (float)tet_solve<double, false>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[3]) { r3 = (float)tet_solve<double, false, false>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[0]) { r0 = (float)tet_solve<double, false, false>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[1]) { r1 = (float)tet_solve<double, false, false>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
+      if (ill[2]) { r2 = (float)tet_solve<double, false, false>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
     }
     out[3] = fminf(TD, r3);
     out[0] = fminf(TA, r0);
@@ -169,7 +169,7 @@ __device__ __forceinline__ void copy_metric(const DevMesh& m, long long c, float
 // differently contracted FMAs could make the check report a drop of more
 // than the tolerance that the following visit never applies, and two
 // patches could re-activate each other without end.
-template <int D1, int MAXT, bool XDIV, int MINB>
+template <int D1, int MAXT, bool XDIV, int MINB, bool PREC>
 __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepParams sp, int cur, int check) {
   const bool CHECK = check != 0;
   extern __shared__ float smem[];
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
       }
       if (act) {
         float nw[4];
-        solve_copy<D1, XDIV>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau, nflag);
+        solve_copy<D1, XDIV, PREC>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau, nflag);
 #pragma unroll
         for (int k = 0; k < D1; ++k) {
           if (idx[k] < nvp) atomicMin(reinterpret_cast<int*>(&sT[idx[k]]), __float_as_int(nw[k]));
@@ -666,22 +666,36 @@ cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float 
   return cudaGetLastError();
 }
 
-// Block size classes: patches of up to 384 element copies run two CTAs per
-// SM (registers capped at 85), larger ones one CTA of 512 or 1024 threads.
+// Block size classes: patches of up to 384 element copies run 2, 3 or 4
+// CTAs per SM (registers capped at 85 / 56 / 42; StepParams::ctas), larger
+// ones one CTA of 512 or 1024 threads.
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
                          const Launch& L, cudaStream_t st) {
   const bool xd = sp.xdiv != 0;
+  const bool pr = sp.tau > 0.f;
   const int c = check ? 1 : 0;
-#define LS_FIM(D, T, X, B) k_fim<D, T, X, B><<<L.fim_grid, L.fim_block, L.fim_smem, st>>>(m, s, sp, cur, c)
+#define LS_FIM(D, T, X, B, P) k_fim<D, T, X, B, P><<<L.fim_grid, L.fim_block, L.fim_smem, st>>>(m, s, sp, cur, c)
+#define LS_FIM3(T, B) \
+  do { \
+    if (xd) { if (pr) LS_FIM(4, T, true, B, true); else LS_FIM(4, T, true, B, false); } \
+    else { if (pr) LS_FIM(4, T, false, B, true); else LS_FIM(4, T, false, B, false); } \
+  } while (0)
   if (m.dim == 3) {
-    if (L.fim_block <= 384) { if (xd) LS_FIM(4, 384, true, 2); else LS_FIM(4, 384, false, 2); }
-    else if (L.fim_block <= 512) { if (xd) LS_FIM(4, 512, true, 1); else LS_FIM(4, 512, false, 1); }
-    else { if (xd) LS_FIM(4, 1024, true, 1); else LS_FIM(4, 1024, false, 1); }
+    if (L.fim_block <= 384) {
+      if (sp.ctas == 2) LS_FIM3(384, 2);
+      else if (sp.ctas == 4) LS_FIM3(384, 4);
+      else LS_FIM3(384, 3);
+    } else if (L.fim_block <= 512) {
+      LS_FIM3(512, 1);
+    } else {
+      LS_FIM3(1024, 1);
+    }
   } else {
-    if (L.fim_block <= 384) LS_FIM(3, 384, false, 2);
-    else if (L.fim_block <= 512) LS_FIM(3, 512, false, 1);
-    else LS_FIM(3, 1024, false, 1);
+    if (L.fim_block <= 384) LS_FIM(3, 384, false, 3, false);
+    else if (L.fim_block <= 512) LS_FIM(3, 512, false, 1, false);
+    else LS_FIM(3, 1024, false, 1, false);
   }
+#undef LS_FIM3
 #undef LS_FIM
   return cudaGetLastError();
 }
@@ -731,19 +745,23 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   L.fim_smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
   int occ = 0;
   if (m.dim == 3) {
-    if (L.fim_block <= 384)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 2>, L.fim_block, L.fim_smem);
+    if (L.fim_block <= 384 && sp.ctas == 2)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 2, false>, L.fim_block, L.fim_smem);
+    else if (L.fim_block <= 384 && sp.ctas == 4)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 4, false>, L.fim_block, L.fim_smem);
+    else if (L.fim_block <= 384)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 3, false>, L.fim_block, L.fim_smem);
     else if (L.fim_block <= 512)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 512, false, 1>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 512, false, 1, false>, L.fim_block, L.fim_smem);
     else
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 1024, false, 1>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 1024, false, 1, false>, L.fim_block, L.fim_smem);
   } else {
     if (L.fim_block <= 384)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 384, false, 2>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 384, false, 3, false>, L.fim_block, L.fim_smem);
     else if (L.fim_block <= 512)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 512, false, 1>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 512, false, 1, false>, L.fim_block, L.fim_smem);
     else
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 1024, false, 1>, L.fim_block, L.fim_smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<3, 1024, false, 1, false>, L.fim_block, L.fim_smem);
   }
   if (e != cudaSuccess) return e;
   if (occ < 1) occ = 1;

@@ -49,6 +49,7 @@ struct SolverConfig {
   int inside_niter = 1;
   int max_fim_iters = 100000;
   int graph_chunk = 4;
+  int fim_ctas = 3;
   double dt = 1.0;
   double bandwidth = 16.0;
   double curv_coeff = 1.0;

@@ -33,7 +33,7 @@ class Params(ctypes.Structure):
         ("update_kind", ctypes.c_int), ("curv_coeff", ctypes.c_double), ("flags", ctypes.c_uint),
         ("fim_sweeps", ctypes.c_int), ("max_fim_iters", ctypes.c_int), ("smallnum", ctypes.c_double),
         ("largenum", ctypes.c_double), ("length_scale", ctypes.c_double), ("fp64_threshold", ctypes.c_double),
-        ("graph_chunk", ctypes.c_int),
+        ("graph_chunk", ctypes.c_int), ("fim_ctas_per_sm", ctypes.c_int),
     ]
 
 
