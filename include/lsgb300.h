@@ -127,6 +127,17 @@ ls_status ls_set_params(ls_handle* h, const ls_params* p);
 ls_status ls_get_params(ls_handle* h, ls_params* p);
 /* initializeMesh: xyz nv*3 floats, elems ne*(3|4) ints (0-based). */
 ls_status ls_set_mesh(ls_handle* h, const float* xyz, int nv, const int* elems, int ne);
+/* initializeMesh from a file (src/LevelSet.cu:111-144): tetgen .node/.ele
+ * (basename or either file) for tet handles, ASCII PLY for triangle handles
+ * (polygons are split into triangle fans).  Tets with negative signed
+ * volume get their last two vertices swapped (TetMesh::reorient, called at
+ * src/LevelSet.cu:139). */
+ls_status ls_load_mesh(ls_handle* h, const char* filename);
+ls_status ls_get_mesh_info(ls_handle* h, int* nv, int* ne);
+ls_status ls_get_mesh(ls_handle* h, float* xyz, int* elems);
+/* writeVTK for one phi (meshFIM3d.cu:48-81): legacy VTK unstructured grid,
+ * POINT_DATA "traveltime". */
+ls_status ls_write_vtk(ls_handle* h, const char* path, const float* phi);
 /* Partition input (replaces Partition_METIS / GraphPartition_Square):
  * npart nv ints in [0, nparts).  Optional; ls_setup partitions otherwise. */
 ls_status ls_set_partition(ls_handle* h, const int* npart, int nparts);
@@ -151,6 +162,12 @@ ls_status ls_step(ls_handle* h, int nsteps, int* steps_done);
 /* End-to-end step through host buffers: phi_in (nv floats, host) is copied
  * to the device, one step runs, phi_out (host) receives the result. */
 ls_status ls_step_host(ls_handle* h, const float* phi_in, float* phi_out);
+/* Standalone eikonal solve (the fast iterative method of the redistance,
+ * without the narrowband limit): distance from the given seed vertices
+ * (caller order, seed values >= 0) over the whole mesh, unit speed.  dist:
+ * nv floats, LARGENUM where unreached.  Overwrites the step state: the next
+ * step searches seeds in every patch. */
+ls_status ls_eikonal(ls_handle* h, const int* seeds, const float* values, int nseeds, float* dist);
 /* Current phi in the caller's vertex order. */
 ls_status ls_get_phi(ls_handle* h, float* phi);
 ls_status ls_get_stats(ls_handle* h, ls_stats* s);

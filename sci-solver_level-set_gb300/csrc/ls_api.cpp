@@ -12,6 +12,7 @@
 
 #include "../../include/lsgb300.h"
 #include "ls_layout.h"
+#include "ls_meshio.h"
 #include "ls_solver.h"
 
 struct ls_handle {
@@ -150,6 +151,38 @@ ls_status ls_set_mesh(ls_handle* h, const float* xyz, int nv, const int* elems, 
   h->have_phi = h->have_vel = false;
   h->layout.reset();
   h->solver.reset();
+  return LS_OK;
+}
+
+ls_status ls_load_mesh(ls_handle* h, const char* filename) {
+  if (!h || !filename) return LS_BAD_INPUT;
+  std::vector<float> xyz;
+  std::vector<int> el;
+  std::string r = lsgb::read_mesh(filename, h->is_tri != 0, xyz, el);
+  if (!r.empty()) return fail(h, LS_BAD_INPUT, r);
+  const int d1 = h->is_tri ? 3 : 4;
+  return ls_set_mesh(h, xyz.data(), (int)(xyz.size() / 3), el.data(), (int)(el.size() / d1));
+}
+
+ls_status ls_get_mesh_info(ls_handle* h, int* nv, int* ne) {
+  if (!h || !nv || !ne) return LS_BAD_INPUT;
+  *nv = h->nv;
+  *ne = h->ne;
+  return LS_OK;
+}
+
+ls_status ls_get_mesh(ls_handle* h, float* xyz, int* elems) {
+  if (!h) return LS_BAD_INPUT;
+  if (xyz) std::memcpy(xyz, h->xyz.data(), sizeof(float) * h->xyz.size());
+  if (elems) std::memcpy(elems, h->elems.data(), sizeof(int) * h->elems.size());
+  return LS_OK;
+}
+
+ls_status ls_write_vtk(ls_handle* h, const char* path, const float* phi) {
+  if (!h || !path || !phi) return LS_BAD_INPUT;
+  if (h->nv == 0) return fail(h, LS_BAD_INPUT, "no mesh");
+  std::string r = lsgb::write_vtk(path, h->xyz, h->elems, h->is_tri ? 3 : 4, phi);
+  if (!r.empty()) return fail(h, LS_BAD_INPUT, r);
   return LS_OK;
 }
 
@@ -314,6 +347,14 @@ ls_status ls_step_host(ls_handle* h, const float* phi_in, float* phi_out) {
   if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
   if (!phi_in || !phi_out) return fail(h, LS_BAD_INPUT, "null buffer");
   return solver_status(h, h->solver->step_host(phi_in, phi_out));
+}
+
+ls_status ls_eikonal(ls_handle* h, const int* seeds, const float* values, int nseeds, float* dist) {
+  if (!h || !dist || nseeds < 0 || (nseeds > 0 && (!seeds || !values))) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  for (int i = 0; i < nseeds; ++i)
+    if (seeds[i] < 0 || seeds[i] >= h->nv || !(values[i] >= 0.f)) return fail(h, LS_BAD_INPUT, "bad seed");
+  return solver_status(h, h->solver->eikonal(seeds, values, nseeds, dist));
 }
 
 ls_status ls_get_phi(ls_handle* h, float* phi) {

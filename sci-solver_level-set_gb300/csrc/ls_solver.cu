@@ -217,7 +217,7 @@ static std::vector<ProfEvent>& prof_pending() {
   return v;
 }
 
-std::string Solver::fim_loop() {
+std::string Solver::fim_loop(const StepParams& sp, bool use_graph) {
   long long launched = 0;
   auto prof = [&](int kind, auto&& fn) -> cudaError_t {
     if (!cfg_.profile) return fn();
@@ -232,14 +232,14 @@ std::string Solver::fim_loop() {
     return e;
   };
   while (true) {
-    if (graph_exec_ && !cfg_.profile) {
+    if (use_graph && graph_exec_ && !cfg_.profile) {
       LS_TRY(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
     } else {
       for (int i = 0; i < cfg_.graph_chunk; ++i) {
         const int cur = i & 1;
-        LS_TRY(prof(0, [&] { return K_->sweep(m_, s_, sp_, cur, false, L_, stream_); }), "sweep");
-        LS_TRY(prof(2, [&] { return K_->schedule(m_, s_, sp_, cur, L_, stream_); }), "schedule");
-        LS_TRY(prof(1, [&] { return K_->sweep(m_, s_, sp_, cur, true, L_, stream_); }), "check");
+        LS_TRY(prof(0, [&] { return K_->sweep(m_, s_, sp, cur, false, L_, stream_); }), "sweep");
+        LS_TRY(prof(2, [&] { return K_->schedule(m_, s_, sp, cur, L_, stream_); }), "schedule");
+        LS_TRY(prof(1, [&] { return K_->sweep(m_, s_, sp, cur, true, L_, stream_); }), "check");
       }
     }
     launched += cfg_.graph_chunk;
@@ -277,7 +277,7 @@ std::string Solver::one_step(bool* empty_nb) {
   LS_TRY(prof(3, [&] { return K_->seed(m_, s_, use_all, sp_.scale, L_, stream_); }), "seed");
   LS_TRY(cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_), "memset");
   st_.kernel_launches += 3;  // reset, seed, narrowband
-  std::string r = fim_loop();
+  std::string r = fim_loop(sp_, true);
   if (!r.empty()) return r;
   LS_TRY(prof(4, [&] { return K_->narrowband(m_, s_, sp_, L_, stream_); }), "narrowband");
   LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
@@ -371,6 +371,49 @@ std::string Solver::step_host(const float* phi_in, float* phi_out) {
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   std::memcpy(phi_out, h_stage_, sizeof(float) * m_.nv);
   if (!empty) st_.steps_run++;
+  pull_stats();
+  return "";
+}
+
+std::string Solver::eikonal(const int* seeds, const float* values, int nseeds, float* out) {
+  const Layout& L = *lay_;
+  const int nv = m_.nv, np = m_.nparts;
+  const float LN = sp_.largenum;
+  std::vector<float> dt(nv, LN);
+  std::vector<uint8_t> sd(nv, 0);
+  std::vector<int> act;
+  for (int i = 0; i < nseeds; ++i) {
+    const int v = L.vert_ipermute[seeds[i]];
+    const float a = values[i];
+    dt[v] = (a >= LN) ? LN : a / sp_.scale;
+    sd[v] = 1;
+  }
+  // first active list: the patches one of whose element copies holds a seed
+  // (the list the seed kernel makes at the start of a time step)
+  const int d1 = m_.dim + 1;
+  for (int p = 0; p < np; ++p) {
+    bool hit = false;
+    for (int c = L.ele_offsets[p]; c < L.ele_offsets[p + 1] && !hit; ++c)
+      for (int k = 0; k < d1; ++k) hit |= sd[L.conn[(size_t)c * d1 + k]] != 0;
+    if (hit) act.push_back(p);
+  }
+  int counts[8] = {(int)act.size(), 0, 0, 0, 0, 0, 0, 0};
+  LS_TRY(cudaMemcpyAsync(s_.DT, dt.data(), sizeof(float) * nv, cudaMemcpyHostToDevice, stream_), "h2d");
+  LS_TRY(cudaMemcpyAsync(s_.seed, sd.data(), nv, cudaMemcpyHostToDevice, stream_), "h2d");
+  if (!act.empty())
+    LS_TRY(cudaMemcpyAsync(s_.list0, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, stream_), "h2d");
+  LS_TRY(cudaMemcpyAsync(s_.counts, counts, sizeof(counts), cudaMemcpyHostToDevice, stream_), "h2d");
+  LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * np, stream_), "memset");
+  StepParams sp = sp_;
+  // no narrowband limit: every converged patch that the front has reached
+  // (minimum below LARGENUM) activates its neighbours
+  sp.bandwidth = LN;
+  std::string r = fim_loop(sp, false);
+  if (!r.empty()) return r;
+  LS_TRY(cudaMemcpyAsync(dt.data(), s_.DT, sizeof(float) * nv, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  for (int v = 0; v < nv; ++v) out[L.vert_permute[v]] = (dt[v] >= LN) ? LN : dt[v] * sp_.scale;
+  have_nb_ = false;  // the step state was overwritten
   pull_stats();
   return "";
 }

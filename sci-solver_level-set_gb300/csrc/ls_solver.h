@@ -81,6 +81,9 @@ class Solver {
   // Run nsteps; history (optional) gets phi after each step (host, caller order).
   std::string run(int nsteps, float* history, int* steps_done);
   std::string step_host(const float* phi_in, float* phi_out);
+  // Distance from arbitrary seed vertices (caller order), whole mesh, no
+  // narrowband limit; out: nv floats in the caller's order.
+  std::string eikonal(const int* seeds, const float* values, int nseeds, float* out);
   std::string narrowband(unsigned char* flags);
   std::string active_patches(std::vector<int>& out);
   std::string dt_values(float* dt_new_order);
@@ -92,7 +95,7 @@ class Solver {
  private:
   std::string check(cudaError_t e, const char* what);
   std::string one_step(bool* empty_nb);
-  std::string fim_loop();
+  std::string fim_loop(const StepParams& sp, bool use_graph);
   std::string build_graph();
   void pull_stats();
 

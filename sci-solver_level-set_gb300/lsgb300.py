@@ -60,7 +60,8 @@ EXPORTS = [
     "ls_set_partition", "ls_set_phi", "ls_set_velocity", "ls_prepare", "ls_setup", "ls_solve", "ls_step",
     "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_narrowband",
     "ls_get_layout_info", "ls_get_layout", "ls_last_error", "ls_version", "ls_partition_structured",
-    "ls_partition_rcb", "ls_set_profile", "ls_debug_active", "ls_narrowband_noalloc",
+    "ls_partition_rcb", "ls_set_profile", "ls_debug_active", "ls_narrowband_noalloc", "ls_load_mesh",
+    "ls_get_mesh_info", "ls_get_mesh", "ls_write_vtk", "ls_eikonal",
 ]
 
 _lib = None
@@ -94,6 +95,11 @@ def lib():
     L.ls_reset_stats.argtypes = [P]
     L.ls_set_profile.argtypes = [P, I]
     L.ls_debug_active.argtypes = [P, V, I, ctypes.POINTER(I), V]
+    L.ls_load_mesh.argtypes = [P, ctypes.c_char_p]
+    L.ls_get_mesh_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.ls_get_mesh.argtypes = [P, V, V]
+    L.ls_write_vtk.argtypes = [P, ctypes.c_char_p, V]
+    L.ls_eikonal.argtypes = [P, V, V, I, V]
     L.ls_narrowband_noalloc.argtypes = [I, I, V, V, V, ctypes.c_float, ctypes.c_float, ctypes.c_float, V, V, V, V]
     L.ls_get_narrowband.argtypes = [P, V]
     L.ls_get_layout_info.argtypes = [P, V]
@@ -185,6 +191,27 @@ class LevelSet:
         self._elems = np.ascontiguousarray(elems, np.int32)
         self.nv, self.ne = len(self._xyz), len(self._elems)
         self._check(lib().ls_set_mesh(self._h, _ptr(self._xyz), self.nv, _ptr(self._elems), self.ne), "set_mesh")
+
+    def load_mesh(self, filename):
+        self._check(lib().ls_load_mesh(self._h, filename.encode()), "load_mesh")
+        nv, ne = ctypes.c_int(0), ctypes.c_int(0)
+        lib().ls_get_mesh_info(self._h, ctypes.byref(nv), ctypes.byref(ne))
+        self.nv, self.ne = nv.value, ne.value
+        self._xyz = np.zeros((self.nv, 3), np.float32)
+        self._elems = np.zeros((self.ne, 3 if self.is_tri else 4), np.int32)
+        lib().ls_get_mesh(self._h, _ptr(self._xyz), _ptr(self._elems))
+        return self._xyz, self._elems
+
+    def write_vtk(self, path, phi):
+        a = np.ascontiguousarray(phi, np.float32)
+        self._check(lib().ls_write_vtk(self._h, path.encode(), _ptr(a)), "write_vtk")
+
+    def eikonal(self, seeds, values):
+        s = np.ascontiguousarray(seeds, np.int32)
+        v = np.ascontiguousarray(values, np.float32)
+        out = np.zeros(self.nv, np.float32)
+        self._check(lib().ls_eikonal(self._h, _ptr(s), _ptr(v), len(s), _ptr(out)), "eikonal")
+        return out
 
     def set_partition(self, npart, nparts):
         a = np.ascontiguousarray(npart, np.int32)

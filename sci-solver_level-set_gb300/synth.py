@@ -166,3 +166,41 @@ def workload(name, seed=0, scale=1.0, n=None):
             vel = (vel.astype(np.float64) * scale).astype(np.float32)
             cfg["dt"] *= 1.0
     return dict(xyz=xyz, elems=el, phi0=phi, vel=vel, npart=npart, nparts=nparts, **cfg)
+
+
+def write_tetgen(base, xyz, tets, first=0):
+    """tetgen .node/.ele pair (index base `first`, with a comment line)."""
+    xyz = np.asarray(xyz, np.float64)
+    with open(base + ".node", "w") as f:
+        f.write("# generated mesh\n%d 3 0 0\n" % len(xyz))
+        for i, p in enumerate(xyz):
+            f.write("%d %.9g %.9g %.9g\n" % (i + first, p[0], p[1], p[2]))
+    with open(base + ".ele", "w") as f:
+        f.write("%d 4 0\n" % len(tets))
+        for i, t in enumerate(np.asarray(tets)):
+            f.write("%d %d %d %d %d\n" % (i + first, t[0] + first, t[1] + first, t[2] + first, t[3] + first))
+
+
+def write_ply(path, xyz, faces):
+    """ASCII PLY; faces is a list of vertex-index sequences (any length >= 3)."""
+    xyz = np.asarray(xyz, np.float64)
+    with open(path, "w") as f:
+        f.write("ply\nformat ascii 1.0\ncomment generated mesh\nelement vertex %d\n" % len(xyz))
+        f.write("property float x\nproperty float y\nproperty float z\n")
+        f.write("element face %d\nproperty list uchar int vertex_indices\nend_header\n" % len(faces))
+        for p in xyz:
+            f.write("%.9g %.9g %.9g\n" % (p[0], p[1], p[2]))
+        for fc in faces:
+            f.write("%d %s\n" % (len(fc), " ".join(str(int(v)) for v in fc)))
+
+
+def reorient(xyz, tets):
+    """Positive signed volume for every tet: swap the last two vertices of
+    the negative ones (the loader's orientation rule)."""
+    xyz = np.asarray(xyz, np.float64)
+    t = np.array(tets, np.int32, copy=True)
+    a, b, c, d = (xyz[t[:, k]] for k in range(4))
+    vol = np.einsum("ij,ij->i", b - a, np.cross(c - a, d - a))
+    neg = vol < 0
+    t[neg, 2], t[neg, 3] = tets[neg, 3], tets[neg, 2]
+    return t
