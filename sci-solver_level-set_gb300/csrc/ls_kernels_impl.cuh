@@ -45,6 +45,8 @@ __global__ void k_reset(DevState s, int nv, float LN) {
 // vertices as seeds with DT = |phi|; the patch joins list0.
 template <int D1>
 __global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
+  // use_all < 0: decided on the device from the step-control flag
+  if (use_all < 0) use_all = s.ctl[2] ? 0 : 1;
   const int count = use_all ? m.nparts : s.counts[3];
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
     const int p = use_all ? li : s.nblist[li];

@@ -150,11 +150,13 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(dalloc(A, &s_.nblist, np), "alloc");
   LS_TRY(dalloc(A, &s_.counts, 8), "alloc");
   LS_TRY(dalloc(A, &s_.stats, 8), "alloc");
+  LS_TRY(dalloc(A, &s_.ctl, 4), "alloc");
   LS_TRY(dalloc(A, &d_tmp_, nv), "alloc");
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 8, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 8, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.ctl, 0, sizeof(int) * 4, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.phi, 0, sizeof(float) * nv, stream_), "memset");
-  LS_TRY(cudaMallocHost((void**)&h_counts_, sizeof(int) * 8), "pinned");
+  LS_TRY(cudaMallocHost((void**)&h_counts_, sizeof(int) * 12), "pinned");
   LS_TRY(cudaMallocHost((void**)&h_stats_, sizeof(unsigned long long) * 8), "pinned");
   LS_TRY(cudaMallocHost((void**)&h_stage_, sizeof(float) * nv), "pinned");
 
@@ -188,18 +190,91 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   return "";
 }
 
+// Step control kernels (host orchestration, same for both kernel builds).
+namespace {
+// End of one FIM loop body (graph_chunk iterations): continue while the
+// active list is not empty, at most max_bodies bodies per step; the cap
+// sets ctl[1] so that the host reports a timeout.
+__global__ void k_loop_cond(const int* counts, int* ctl, cudaGraphConditionalHandle h, int max_bodies) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const int b = ++ctl[0];
+    const bool more = counts[0] > 0;
+    if (more && b >= max_bodies) ctl[1] = 1;
+    cudaGraphSetConditional(h, (more && b < max_bodies) ? 1u : 0u);
+  }
+}
+// After the narrowband: the next step's seed search is restricted to it
+// when it is not empty.
+__global__ void k_step_tail(const int* counts, int* ctl) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) ctl[2] = counts[3] > 0 ? 1 : 0;
+}
+}  // namespace
+
+// One time step as one graph: seed part, a while node running FIM loop
+// bodies of graph_chunk iterations until the active list drains (or the
+// iteration cap), then narrowband and update.  The host launches it and
+// reads the counters once per step.
 std::string Solver::build_graph() {
-  LS_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
+  const int chunk = cfg_.graph_chunk;
+  const int max_bodies = (cfg_.max_fim_iters + chunk - 1) / chunk;
+  cudaGraph_t pre = nullptr, post = nullptr;
   cudaError_t err = cudaSuccess;
-  for (int i = 0; i < cfg_.graph_chunk && err == cudaSuccess; ++i) {
+  // seed part
+  LS_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
+  err = cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.ctl, 0, sizeof(int) * 2, stream_);
+  if (err == cudaSuccess) err = K_->reset(m_, s_, sp_, L_, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_);
+  if (err == cudaSuccess) err = K_->seed(m_, s_, -1, sp_.scale, L_, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_);
+  cudaError_t e2 = cudaStreamEndCapture(stream_, &pre);
+  LS_TRY(err, "capture seed part");
+  LS_TRY(e2, "capture end");
+  // narrowband + update part
+  LS_TRY(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
+  err = K_->narrowband(m_, s_, sp_, L_, stream_);
+  if (err == cudaSuccess) {
+    k_step_tail<<<1, 32, 0, stream_>>>(s_.counts, s_.ctl);
+    err = cudaGetLastError();
+  }
+  if (cfg_.update_kind != 2)
+    for (int it = 0; it < cfg_.inside_niter && err == cudaSuccess; ++it) err = K_->update(m_, s_, sp_, L_, stream_);
+  e2 = cudaStreamEndCapture(stream_, &post);
+  LS_TRY(err, "capture update part");
+  LS_TRY(e2, "capture end");
+
+  LS_TRY(cudaGraphCreate(&graph_, 0), "graph create");
+  cudaGraphNode_t npre, nloop, npost;
+  LS_TRY(cudaGraphAddChildGraphNode(&npre, graph_, nullptr, 0, pre), "graph child");
+  cudaGraphConditionalHandle hc;
+  LS_TRY(cudaGraphConditionalHandleCreate(&hc, graph_, 1, cudaGraphCondAssignDefault), "conditional handle");
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hc;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  LS_TRY(cudaGraphAddNode(&nloop, graph_, &npre, nullptr, 1, &cp), "graph while node");
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  LS_TRY(cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+         "capture body");
+  err = cudaSuccess;
+  for (int i = 0; i < chunk && err == cudaSuccess; ++i) {
     const int cur = i & 1;
     err = K_->sweep(m_, s_, sp_, cur, false, L_, stream_);
     if (err == cudaSuccess) err = K_->schedule(m_, s_, sp_, cur, L_, stream_);
     if (err == cudaSuccess) err = K_->sweep(m_, s_, sp_, cur, true, L_, stream_);
   }
-  cudaError_t e2 = cudaStreamEndCapture(stream_, &graph_);
-  LS_TRY(err, "capture launch");
-  LS_TRY(e2, "capture end");
+  if (err == cudaSuccess) {
+    k_loop_cond<<<1, 32, 0, stream_>>>(s_.counts, s_.ctl, hc, max_bodies);
+    err = cudaGetLastError();
+  }
+  e2 = cudaStreamEndCapture(stream_, &body);
+  LS_TRY(err, "capture body launch");
+  LS_TRY(e2, "capture body end");
+  LS_TRY(cudaGraphAddChildGraphNode(&npost, graph_, &nloop, 1, post), "graph child");
+  cudaGraphDestroy(pre);
+  cudaGraphDestroy(post);
   LS_TRY(cudaGraphInstantiate(&graph_exec_, graph_, 0), "graph instantiate");
   return "";
 }
@@ -217,7 +292,7 @@ static std::vector<ProfEvent>& prof_pending() {
   return v;
 }
 
-std::string Solver::fim_loop(const StepParams& sp, bool use_graph) {
+std::string Solver::fim_loop(const StepParams& sp) {
   long long launched = 0;
   auto prof = [&](int kind, auto&& fn) -> cudaError_t {
     if (!cfg_.profile) return fn();
@@ -232,15 +307,11 @@ std::string Solver::fim_loop(const StepParams& sp, bool use_graph) {
     return e;
   };
   while (true) {
-    if (use_graph && graph_exec_ && !cfg_.profile) {
-      LS_TRY(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
-    } else {
-      for (int i = 0; i < cfg_.graph_chunk; ++i) {
-        const int cur = i & 1;
-        LS_TRY(prof(0, [&] { return K_->sweep(m_, s_, sp, cur, false, L_, stream_); }), "sweep");
-        LS_TRY(prof(2, [&] { return K_->schedule(m_, s_, sp, cur, L_, stream_); }), "schedule");
-        LS_TRY(prof(1, [&] { return K_->sweep(m_, s_, sp, cur, true, L_, stream_); }), "check");
-      }
+    for (int i = 0; i < cfg_.graph_chunk; ++i) {
+      const int cur = i & 1;
+      LS_TRY(prof(0, [&] { return K_->sweep(m_, s_, sp, cur, false, L_, stream_); }), "sweep");
+      LS_TRY(prof(2, [&] { return K_->schedule(m_, s_, sp, cur, L_, stream_); }), "schedule");
+      LS_TRY(prof(1, [&] { return K_->sweep(m_, s_, sp, cur, true, L_, stream_); }), "check");
     }
     launched += cfg_.graph_chunk;
     st_.kernel_launches += 3LL * cfg_.graph_chunk;
@@ -269,6 +340,22 @@ std::string Solver::one_step(bool* empty_nb) {
     prof_pending().push_back(pe);
     return e;
   };
+  if (graph_exec_ && !cfg_.profile) {
+    LS_TRY(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
+    LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaMemcpyAsync(h_counts_ + 8, s_.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaStreamSynchronize(stream_), "step sync");
+    const int bodies = h_counts_[8];
+    st_.kernel_launches += 5LL + (3LL * cfg_.graph_chunk + 1) * bodies +
+                           (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0);
+    if (h_counts_[9]) {
+      status_ = 3;
+      return "FIM did not converge within max_fim_iters iterations";
+    }
+    have_nb_ = h_counts_[3] != 0;
+    *empty_nb = !have_nb_;
+    return "";
+  }
   const int use_all = have_nb_ ? 0 : 1;
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_), "memset");
@@ -276,10 +363,12 @@ std::string Solver::one_step(bool* empty_nb) {
   LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_), "memset");
   LS_TRY(prof(3, [&] { return K_->seed(m_, s_, use_all, sp_.scale, L_, stream_); }), "seed");
   LS_TRY(cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_), "memset");
-  st_.kernel_launches += 3;  // reset, seed, narrowband
-  std::string r = fim_loop(sp_, true);
+  st_.kernel_launches += 4;  // reset, seed, narrowband, step tail
+  std::string r = fim_loop(sp_);
   if (!r.empty()) return r;
   LS_TRY(prof(4, [&] { return K_->narrowband(m_, s_, sp_, L_, stream_); }), "narrowband");
+  k_step_tail<<<1, 32, 0, stream_>>>(s_.counts, s_.ctl);
+  LS_TRY(cudaGetLastError(), "step tail");
   LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
   LS_TRY(cudaStreamSynchronize(stream_), "nb sync");
   if (h_counts_[3] == 0) {
@@ -404,11 +493,12 @@ std::string Solver::eikonal(const int* seeds, const float* values, int nseeds, f
     LS_TRY(cudaMemcpyAsync(s_.list0, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, stream_), "h2d");
   LS_TRY(cudaMemcpyAsync(s_.counts, counts, sizeof(counts), cudaMemcpyHostToDevice, stream_), "h2d");
   LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * np, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.ctl + 2, 0, sizeof(int), stream_), "memset");
   StepParams sp = sp_;
   // no narrowband limit: every converged patch that the front has reached
   // (minimum below LARGENUM) activates its neighbours
   sp.bandwidth = LN;
-  std::string r = fim_loop(sp, false);
+  std::string r = fim_loop(sp);
   if (!r.empty()) return r;
   LS_TRY(cudaMemcpyAsync(dt.data(), s_.DT, sizeof(float) * nv, cudaMemcpyDeviceToHost, stream_), "d2h");
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
@@ -422,6 +512,7 @@ std::string Solver::set_phi(const float* phi_orig) {
   std::memcpy(h_stage_, phi_orig, sizeof(float) * m_.nv);
   LS_TRY(cudaMemcpyAsync(d_tmp_, h_stage_, sizeof(float) * m_.nv, cudaMemcpyHostToDevice, stream_), "h2d");
   LS_TRY(K_->permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
+  LS_TRY(cudaMemsetAsync(s_.ctl + 2, 0, sizeof(int), stream_), "memset");
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   have_nb_ = false;
   return "";

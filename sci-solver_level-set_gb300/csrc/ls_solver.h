@@ -95,7 +95,7 @@ class Solver {
  private:
   std::string check(cudaError_t e, const char* what);
   std::string one_step(bool* empty_nb);
-  std::string fim_loop(const StepParams& sp, bool use_graph);
+  std::string fim_loop(const StepParams& sp);
   std::string build_graph();
   void pull_stats();
 
@@ -110,7 +110,7 @@ class Solver {
   cudaGraphExec_t graph_exec_ = nullptr;
   cudaGraph_t graph_ = nullptr;
   std::vector<void*> allocs_;
-  int* h_counts_ = nullptr;           // pinned mirror of s_.counts
+  int* h_counts_ = nullptr;           // pinned mirror of s_.counts [0..7] and s_.ctl [8..11]
   unsigned long long* h_stats_ = nullptr;
   float* h_stage_ = nullptr;          // pinned nv floats
   float* d_tmp_ = nullptr;            // nv floats (caller-order staging)
