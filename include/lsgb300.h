@@ -238,6 +238,38 @@ ls_status ls_partition_structured(int dim, int nside, int block, int nv, int* np
  * max(2, nv / target) parts (2D, meshFIM2d.cu:380-382). */
 ls_status ls_partition_rcb(int dim, const float* xyz, int nv, int target, int* npart, int* nparts);
 
+/* Batches of independent meshes (no counterpart in the reference, which
+ * solves one mesh per LevelSet and process).  Each member is a handle with
+ * its mesh, partition, phi0, velocity and parameters set; ls_batch_add
+ * prepares it (ls_prepare) and copies what the batch needs, so the handle
+ * may be destroyed afterwards.  The members' patch layouts are merged into
+ * one patch set: every FIM iteration, narrowband and update launch covers
+ * all members at once, each with its own time step, bandwidth, curvature
+ * coefficient and FIM length unit.  Members must share the update kind, the
+ * flags (LS_PROFILE aside), fim_sweeps, inside_iterations, smallnum,
+ * largenum and fp64_threshold; the first member's graph_chunk,
+ * max_fim_iters and fim_ctas_per_sm apply.  A step of the batch is one step
+ * of every member; solving stops early only when every member's narrowband
+ * is empty, and a member whose narrowband empties earlier keeps the
+ * +-LARGENUM values that its empty redistance leaves. */
+typedef struct ls_batch ls_batch;
+ls_status ls_batch_create(ls_batch** b);
+ls_status ls_batch_destroy(ls_batch* b);
+const char* ls_batch_last_error(ls_batch* b);
+/* index: position of the member (0, 1, ...) */
+ls_status ls_batch_add(ls_batch* b, ls_handle* h, int* index);
+ls_status ls_batch_setup(ls_batch* b);
+ls_status ls_batch_solve(ls_batch* b, int nsteps, int* steps_done);
+/* phi of one member, in that member's vertex order */
+ls_status ls_batch_get_phi(ls_batch* b, int index, float* phi);
+ls_status ls_batch_get_stats(ls_batch* b, ls_stats* s);
+ls_status ls_batch_reset_stats(ls_batch* b);
+ls_status ls_batch_set_profile(ls_batch* b, int on);
+/* merged layout (host only; same info[10] and LS_REF_* arrays as
+ * ls_get_layout_info / ls_get_layout) */
+ls_status ls_batch_get_layout_info(ls_batch* b, long long* info);
+ls_status ls_batch_get_layout(ls_batch* b, int which, void* dst);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,25 @@ struct ls_handle {
   std::string err;
 };
 
+// A batch of independent meshes stepped together (no counterpart in the
+// reference): the members' layouts are merged into one patch set, so every
+// FIM iteration, narrowband and update pass covers all meshes at once.
+struct ls_batch {
+  struct Member {
+    lsgb::Layout layout;
+    std::vector<float> phi, vel;
+    ls_params prm;
+    int nv = 0, ne = 0;
+  };
+  std::vector<Member> members;
+  int is_tri = -1;
+  std::vector<int> vbase;  // first vertex of each member in the merged numbering
+  std::unique_ptr<lsgb::Layout> layout;
+  std::unique_ptr<lsgb::Solver> solver;
+  std::vector<float> stage;
+  std::string err;
+};
+
 namespace {
 ls_status fail(ls_handle* h, ls_status s, const std::string& msg) {
   if (h) h->err = msg;
@@ -71,6 +90,48 @@ void rcb(const float* xyz, std::vector<int>& idx, int lo, int hi, int nparts, in
   });
   rcb(xyz, idx, lo, mid, left, first, npart);
   rcb(xyz, idx, mid, hi, nparts - left, first + left, npart);
+}
+
+void fill_stats(const lsgb::SolverStats& t, ls_stats* s) {
+  s->steps_run = (int)t.steps_run;
+  s->fim_iters = t.fim_iters;
+  s->patch_visits = t.patch_visits;
+  s->check_visits = t.check_visits;
+  s->nb_vertex_updates = t.nb_vertex_updates;
+  s->nb_patch_vertices = t.nb_patch_vertices;
+  s->nb_patches = t.nb_patches;
+  s->flagged_copies = t.flagged_copies;
+  s->ms_total = t.ms_total;
+  s->ms_sweep = t.ms_sweep; s->ms_check = t.ms_check; s->ms_schedule = t.ms_schedule;
+  s->ms_seed = t.ms_seed; s->ms_narrowband = t.ms_narrowband; s->ms_update = t.ms_update;
+  s->n_sweep = t.n_sweep; s->n_check = t.n_check; s->n_schedule = t.n_schedule;
+  s->n_seed = t.n_seed; s->n_narrowband = t.n_narrowband; s->n_update = t.n_update;
+  s->sweep_slab_bytes = t.sweep_slab_bytes;
+  s->kernel_launches = t.kernel_launches;
+}
+
+// Solver configuration from a handle's parameters.
+lsgb::SolverConfig solver_config(const ls_params& p) {
+  lsgb::SolverConfig cfg;
+  cfg.update_kind = p.update_kind;
+  cfg.ref_compat = (p.flags & LS_REF_COMPAT) ? 1 : 0;
+  cfg.fp64_flagged = (p.flags & LS_FP64_FLAGGED) ? 1 : 0;
+  cfg.profile = (p.flags & LS_PROFILE) ? 1 : 0;
+  cfg.use_graph = (p.flags & LS_NO_GRAPH) ? 0 : 1;
+  cfg.bit_exact = (p.flags & LS_BITEXACT) ? 1 : 0;
+  cfg.niter = p.fim_sweeps;
+  cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
+  cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;
+  cfg.graph_chunk = p.graph_chunk > 0 ? p.graph_chunk : 4;
+  cfg.fim_ctas = p.fim_ctas_per_sm > 0 ? p.fim_ctas_per_sm : 3;
+  cfg.dt = p.time_step;
+  cfg.bandwidth = p.bandwidth;
+  cfg.curv_coeff = p.curv_coeff;
+  cfg.smallnum = p.smallnum > 0 ? p.smallnum : 1e-5;
+  cfg.largenum = p.largenum > 0 ? p.largenum : 1e9;
+  cfg.length_scale = p.length_scale;
+  if (p.fp64_threshold > 0) cfg.fp64_tau = p.fp64_threshold;
+  return cfg;
 }
 }  // namespace
 
@@ -303,26 +364,7 @@ ls_status ls_prepare(ls_handle* h) {
 ls_status ls_setup(ls_handle* h) {
   ls_status ps = ls_prepare(h);
   if (ps != LS_OK) return ps;
-  lsgb::SolverConfig cfg;
-  const ls_params& p = h->prm;
-  cfg.update_kind = p.update_kind;
-  cfg.ref_compat = (p.flags & LS_REF_COMPAT) ? 1 : 0;
-  cfg.fp64_flagged = (p.flags & LS_FP64_FLAGGED) ? 1 : 0;
-  cfg.profile = (p.flags & LS_PROFILE) ? 1 : 0;
-  cfg.use_graph = (p.flags & LS_NO_GRAPH) ? 0 : 1;
-  cfg.bit_exact = (p.flags & LS_BITEXACT) ? 1 : 0;
-  cfg.niter = p.fim_sweeps;
-  cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
-  cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;
-  cfg.graph_chunk = p.graph_chunk > 0 ? p.graph_chunk : 4;
-  cfg.fim_ctas = p.fim_ctas_per_sm > 0 ? p.fim_ctas_per_sm : 3;
-  cfg.dt = p.time_step;
-  cfg.bandwidth = p.bandwidth;
-  cfg.curv_coeff = p.curv_coeff;
-  cfg.smallnum = p.smallnum > 0 ? p.smallnum : 1e-5;
-  cfg.largenum = p.largenum > 0 ? p.largenum : 1e9;
-  cfg.length_scale = p.length_scale;
-  if (p.fp64_threshold > 0) cfg.fp64_tau = p.fp64_threshold;
+  lsgb::SolverConfig cfg = solver_config(h->prm);
   h->solver = std::make_unique<lsgb::Solver>();
   std::string r = h->solver->init(*h->layout, cfg, h->vel.data());
   if (!r.empty()) {
@@ -369,21 +411,7 @@ ls_status ls_get_stats(ls_handle* h, ls_stats* s) {
   if (!h->solver) return LS_OK;
   lsgb::SolverStats t;
   h->solver->stats(t);
-  s->steps_run = (int)t.steps_run;
-  s->fim_iters = t.fim_iters;
-  s->patch_visits = t.patch_visits;
-  s->check_visits = t.check_visits;
-  s->nb_vertex_updates = t.nb_vertex_updates;
-  s->nb_patch_vertices = t.nb_patch_vertices;
-  s->nb_patches = t.nb_patches;
-  s->flagged_copies = t.flagged_copies;
-  s->ms_total = t.ms_total;
-  s->ms_sweep = t.ms_sweep; s->ms_check = t.ms_check; s->ms_schedule = t.ms_schedule;
-  s->ms_seed = t.ms_seed; s->ms_narrowband = t.ms_narrowband; s->ms_update = t.ms_update;
-  s->n_sweep = t.n_sweep; s->n_check = t.n_check; s->n_schedule = t.n_schedule;
-  s->n_seed = t.n_seed; s->n_narrowband = t.n_narrowband; s->n_update = t.n_update;
-  s->sweep_slab_bytes = t.sweep_slab_bytes;
-  s->kernel_launches = t.kernel_launches;
+  fill_stats(t, s);
   return LS_OK;
 }
 
@@ -433,6 +461,170 @@ ls_status ls_get_layout(ls_handle* h, int which, void* dst) {
   if (!h || !dst) return LS_BAD_INPUT;
   if (!h->layout) return fail(h, LS_NOT_READY, "call ls_setup first");
   if (!lsgb::ref_array_copy(*h->layout, which, dst)) return fail(h, LS_BAD_INPUT, "unknown layout array");
+  return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of independent meshes.
+
+namespace {
+ls_status bfail(ls_batch* b, ls_status s, const std::string& msg) {
+  if (b) b->err = msg;
+  return s;
+}
+ls_status bsolver_status(ls_batch* b, const std::string& msg) {
+  if (msg.empty()) return LS_OK;
+  b->err = msg;
+  switch (b->solver ? b->solver->status_code() : 4) {
+    case 1: return LS_BAD_INPUT;
+    case 2: return LS_PATCH_TOO_LARGE;
+    case 3: return LS_DEVICE_TIMEOUT;
+    default: return LS_CUDA_ERROR;
+  }
+}
+}  // namespace
+
+ls_status ls_batch_create(ls_batch** b) {
+  if (!b) return LS_BAD_INPUT;
+  *b = new (std::nothrow) ls_batch();
+  return *b ? LS_OK : LS_NO_MEMORY;
+}
+
+ls_status ls_batch_destroy(ls_batch* b) {
+  delete b;
+  return LS_OK;
+}
+
+const char* ls_batch_last_error(ls_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+ls_status ls_batch_add(ls_batch* b, ls_handle* h, int* index) {
+  if (!b || !h) return LS_BAD_INPUT;
+  if (b->solver) return bfail(b, LS_BAD_INPUT, "batch already set up");
+  ls_status s = ls_prepare(h);
+  if (s != LS_OK) return bfail(b, s, std::string("member: ") + h->err);
+  if (b->is_tri < 0) b->is_tri = h->is_tri;
+  if (h->is_tri != b->is_tri) return bfail(b, LS_BAD_INPUT, "members of different dimension");
+  if (!b->members.empty()) {
+    const ls_params& a = b->members[0].prm;
+    const ls_params& q = h->prm;
+    const unsigned mask = ~(unsigned)LS_PROFILE;
+    if (a.update_kind != q.update_kind || (a.flags & mask) != (q.flags & mask) || a.fim_sweeps != q.fim_sweeps ||
+        a.inside_iterations != q.inside_iterations || a.smallnum != q.smallnum || a.largenum != q.largenum ||
+        a.fp64_threshold != q.fp64_threshold)
+      return bfail(b, LS_BAD_INPUT, "members must share the update kind, flags, sweeps and constants");
+  }
+  ls_batch::Member m;
+  m.layout = *h->layout;
+  m.phi = h->phi;
+  m.vel = h->vel;
+  m.prm = h->prm;
+  m.nv = h->nv;
+  m.ne = h->ne;
+  b->members.push_back(std::move(m));
+  if (index) *index = (int)b->members.size() - 1;
+  return LS_OK;
+}
+
+ls_status ls_batch_setup(ls_batch* b) {
+  if (!b) return LS_BAD_INPUT;
+  if (b->members.empty()) return bfail(b, LS_BAD_INPUT, "empty batch");
+  std::vector<const lsgb::Layout*> parts;
+  for (auto& m : b->members) parts.push_back(&m.layout);
+  auto L = std::make_unique<lsgb::Layout>();
+  std::string r = lsgb::merge_layouts(parts, *L);
+  if (!r.empty()) return bfail(b, LS_BAD_INPUT, r);
+  lsgb::SolverConfig cfg = solver_config(b->members[0].prm);
+  std::vector<float> vel, phi;
+  b->vbase.clear();
+  int vb = 0;
+  for (auto& m : b->members) {
+    cfg.mesh_dt.push_back(m.prm.time_step);
+    cfg.mesh_bandwidth.push_back(m.prm.bandwidth);
+    cfg.mesh_curv.push_back(m.prm.curv_coeff);
+    cfg.mesh_length_scale.push_back(m.prm.length_scale);
+    vel.insert(vel.end(), m.vel.begin(), m.vel.end());
+    phi.insert(phi.end(), m.phi.begin(), m.phi.end());
+    b->vbase.push_back(vb);
+    vb += m.nv;
+  }
+  b->vbase.push_back(vb);
+  b->layout = std::move(L);
+  b->solver = std::make_unique<lsgb::Solver>();
+  r = b->solver->init(*b->layout, cfg, vel.data());
+  if (!r.empty()) {
+    ls_status s = bsolver_status(b, r);
+    b->solver.reset();
+    return s;
+  }
+  b->stage.assign(vb, 0.f);
+  return bsolver_status(b, b->solver->set_phi(phi.data()));
+}
+
+ls_status ls_batch_solve(ls_batch* b, int nsteps, int* steps_done) {
+  if (!b) return LS_BAD_INPUT;
+  if (!b->solver) return bfail(b, LS_NOT_READY, "call ls_batch_setup first");
+  if (nsteps < 0) return bfail(b, LS_BAD_INPUT, "negative step count");
+  return bsolver_status(b, b->solver->run(nsteps, nullptr, steps_done));
+}
+
+ls_status ls_batch_get_phi(ls_batch* b, int index, float* phi) {
+  if (!b || !phi) return LS_BAD_INPUT;
+  if (!b->solver) return bfail(b, LS_NOT_READY, "call ls_batch_setup first");
+  if (index < 0 || index >= (int)b->members.size()) return bfail(b, LS_BAD_INPUT, "bad member index");
+  std::string r = b->solver->get_phi(b->stage.data());
+  if (!r.empty()) return bsolver_status(b, r);
+  std::memcpy(phi, b->stage.data() + b->vbase[index], sizeof(float) * (size_t)b->members[index].nv);
+  return LS_OK;
+}
+
+ls_status ls_batch_get_stats(ls_batch* b, ls_stats* s) {
+  if (!b || !s) return LS_BAD_INPUT;
+  std::memset(s, 0, sizeof(*s));
+  if (!b->solver) return LS_OK;
+  lsgb::SolverStats t;
+  b->solver->stats(t);
+  fill_stats(t, s);
+  return LS_OK;
+}
+
+ls_status ls_batch_reset_stats(ls_batch* b) {
+  if (!b) return LS_BAD_INPUT;
+  if (b->solver) b->solver->reset_stats();
+  return LS_OK;
+}
+
+ls_status ls_batch_set_profile(ls_batch* b, int on) {
+  if (!b) return LS_BAD_INPUT;
+  if (!b->solver) return bfail(b, LS_NOT_READY, "call ls_batch_setup first");
+  b->solver->set_profile(on != 0);
+  return LS_OK;
+}
+
+ls_status ls_batch_get_layout_info(ls_batch* b, long long* info) {
+  if (!b || !info) return LS_BAD_INPUT;
+  if (!b->layout) {
+    // merge on the host only (no device work), for layout checks
+    std::vector<const lsgb::Layout*> parts;
+    for (auto& m : b->members) parts.push_back(&m.layout);
+    if (parts.empty()) return bfail(b, LS_BAD_INPUT, "empty batch");
+    auto L = std::make_unique<lsgb::Layout>();
+    std::string r = lsgb::merge_layouts(parts, *L);
+    if (!r.empty()) return bfail(b, LS_BAD_INPUT, r);
+    b->layout = std::move(L);
+  }
+  const lsgb::Layout& L = *b->layout;
+  info[0] = L.nparts; info[1] = L.full; info[2] = L.lep; info[3] = L.lvp; info[4] = L.lgp;
+  info[5] = L.lim; info[6] = lsgb::ref_array_size(L, lsgb::REF_BLOCK_ADJNCY); info[7] = L.nv;
+  info[8] = L.ne; info[9] = L.dim;
+  return LS_OK;
+}
+
+ls_status ls_batch_get_layout(ls_batch* b, int which, void* dst) {
+  if (!b || !dst) return LS_BAD_INPUT;
+  long long info[10];
+  ls_status s = ls_batch_get_layout_info(b, info);
+  if (s != LS_OK) return s;
+  if (!lsgb::ref_array_copy(*b->layout, which, dst)) return bfail(b, LS_BAD_INPUT, "unknown layout array");
   return LS_OK;
 }
 

@@ -35,6 +35,17 @@ struct DevMesh {
   const float* xyz;          // SoA [3][nv]
   const int* ipermute;       // old -> new vertex id
   const int* patch_bytes;    // per patch: algorithmic bytes of one FIM visit
+  // batches of independent meshes: mesh of each patch and per-mesh
+  // parameters {bandwidth in the FIM frame, FIM frame scale, dt, curvature
+  // coefficient}; null for a single mesh (StepParams hold them)
+  const int* patch_mesh;
+  const float4* mesh_par;
+};
+
+// Bandwidth (FIM frame), FIM frame scale, dt and curvature coefficient of
+// patch p.
+struct PatchPar {
+  float bw, scale, dt, cc;
 };
 
 // Device step state.
@@ -75,6 +86,15 @@ struct StepParams {
   int update_kind; // 0 advect, 1 curvature
   int lvp, lgp, lep;
 };
+
+__device__ __forceinline__ PatchPar patch_par(const DevMesh& m, const StepParams& sp, int p) {
+  if (m.patch_mesh) {
+    const float4 q = __ldg(&m.mesh_par[__ldg(&m.patch_mesh[p])]);
+    return PatchPar{q.x, q.y, q.z, q.w};
+  }
+  return PatchPar{sp.bandwidth, sp.scale, sp.dt, sp.curv_coeff};
+}
+
 
 enum { LS_FAR = 0, LS_ACTIVE = 1 };
 

@@ -50,6 +50,7 @@ __global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
   const int count = use_all ? m.nparts : s.counts[3];
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
     const int p = use_all ? li : s.nblist[li];
+    const float sc = m.patch_mesh ? __ldg(&m.mesh_par[m.patch_mesh[p]]).y : scale;
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p];
     const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
@@ -72,7 +73,7 @@ __global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
       for (int k = 0; k < D1; ++k) {
         if (cross || val[k] == 0.f) {
           s.seed[gv[k]] = 1;
-          s.DT[gv[k]] = fabsf(val[k]) / scale;
+          s.DT[gv[k]] = fabsf(val[k]) / sc;
           found = 1;
         }
       }
@@ -296,7 +297,7 @@ __global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
         const int pos = atomicAdd(&s.counts[nxt], 1);
         nlist[pos] = p;
       }
-    } else if (s.bmin[p] < sp.bandwidth) {
+    } else if (s.bmin[p] < patch_par(m, sp, p).bw) {
       const int a = m.padj_off[p], b = m.padj_off[p + 1];
       for (int j0 = a; j0 < b; j0 += 32) {
         const int j = j0 + lane;
@@ -330,16 +331,17 @@ __global__ void k_narrowband(DevMesh m, DevState s, StepParams sp) {
   unsigned cnt = 0, pv = 0, npc = 0;
   for (int p = warp_id_global(); p < m.nparts; p += nwarps) {
     const int vs = m.vert_off[p], ve = m.vert_off[p + 1];
+    const PatchPar pp = patch_par(m, sp, p);
     unsigned mn = 0x7f800000u;
     for (int v = vs + lane; v < ve; v += 32) {
       const float d = s.DT[v];
       mn = min(mn, __float_as_uint(d));
-      cnt += (d <= sp.bandwidth);
-      const float mag = (d >= sp.largenum || sp.scale == 1.f) ? d : d * sp.scale;
+      cnt += (d <= pp.bw);
+      const float mag = (d >= sp.largenum || pp.scale == 1.f) ? d : d * pp.scale;
       s.phi[v] = s.sign[v] ? mag : -mag;
     }
     mn = __reduce_min_sync(0xffffffffu, mn);
-    if (lane == 0 && __uint_as_float(mn) <= sp.bandwidth) {
+    if (lane == 0 && __uint_as_float(mn) <= pp.bw) {
       const int pos = atomicAdd(&s.counts[3], 1);
       s.nblist[pos] = p;
       pv += ve - vs;
@@ -563,6 +565,7 @@ __global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParam
   const int count = s.counts[3];
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
     const int p = s.nblist[li];
+    const PatchPar pp = patch_par(m, sp, p);
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
     const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
@@ -605,7 +608,7 @@ __global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParam
           const int sl = m.vslot[q];
           down += sC[(sl >> 2) * stride + 4 + (sl & 3)];
         }
-        if ((double)fabsf(down) > 1e-8) res = oldT - sp.dt * (up / down);
+        if ((double)fabsf(down) > 1e-8) res = oldT - pp.dt * (up / down);
       } else {
         float down = 0.f, gd = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, cu = 0.f;
         for (int q = a; q < b; ++q) {
@@ -620,10 +623,10 @@ __global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParam
         }
         const float node_eik = sqrtf(g0 * g0 + g1 * g1 + g2 * g2) / gd;
         if (sp.ref_compat && D1 == 4) {
-          if ((double)fabsf(down) > 1e-16) res = oldT - sp.curv_coeff * node_eik * (cu / gd) * sp.dt;
+          if ((double)fabsf(down) > 1e-16) res = oldT - pp.cc * node_eik * (cu / gd) * pp.dt;
         } else if (gd > 0.f) {
           // the reference's normalisation (curv_up / sum of element volumes)
-          res = oldT - sp.curv_coeff * node_eik * (cu / gd) * sp.dt;
+          res = oldT - pp.cc * node_eik * (cu / gd) * pp.dt;
         }
       }
       s.phi_out[v] = res;

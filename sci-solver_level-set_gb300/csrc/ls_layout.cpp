@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 
 namespace lsgb {
@@ -222,6 +223,70 @@ std::string build_layout(int dim, int nv, const float* xyz, int ne, const int* e
       L.padj_off[p + 1] = (int)L.padj.size();
     }
   }
+  return "";
+}
+
+std::string merge_layouts(const std::vector<const Layout*>& parts, Layout& out) {
+  out = Layout();
+  if (parts.empty()) return "no meshes";
+  const int dim = parts[0]->dim;
+  long long nv = 0, ne = 0, np = 0, full = 0, ng = 0, ns = 0, na = 0;
+  for (const Layout* P : parts) {
+    if (P->dim != dim) return "meshes of different dimension";
+    nv += P->nv; ne += P->ne; np += P->nparts; full += P->full;
+    ng += (long long)P->ghost_ids.size(); ns += (long long)P->vslot.size(); na += (long long)P->padj.size();
+  }
+  if (nv > INT32_MAX || ne > INT32_MAX || np > INT32_MAX || full > INT32_MAX || ng > INT32_MAX || ns > INT32_MAX ||
+      na > INT32_MAX)
+    return "batch too large for 32-bit indices";
+  out.dim = dim;
+  out.nv = (int)nv; out.ne = (int)ne; out.nparts = (int)np; out.full = full;
+  const int d1 = dim + 1;
+  out.vert_permute.reserve(nv); out.vert_ipermute.reserve(nv);
+  out.vert_offsets.reserve(np + 1); out.ele_offsets.reserve(np + 1);
+  out.ghost_offsets.reserve(np + 1); out.padj_off.reserve(np + 1);
+  out.vslot_off.reserve(nv + 1);
+  out.ele_permute.reserve(full); out.conn.reserve(full * d1); out.conn_local.reserve(full * 4);
+  out.ghost_ids.reserve(ng); out.vslot.reserve(ns); out.padj.reserve(na);
+  out.xyz_p.assign((size_t)nv * 3, 0.f);
+  out.patch_mesh.reserve(np);
+  out.vert_offsets.push_back(0); out.ele_offsets.push_back(0); out.ghost_offsets.push_back(0);
+  out.padj_off.push_back(0); out.vslot_off.push_back(0);
+  int vb = 0, eb = 0, pb = 0, cb = 0, gb = 0, sb = 0, ab = 0;
+  for (size_t k = 0; k < parts.size(); ++k) {
+    const Layout& P = *parts[k];
+    for (int v = 0; v < P.nv; ++v) {
+      out.vert_permute.push_back(vb + P.vert_permute[v]);
+      out.vert_ipermute.push_back(vb + P.vert_ipermute[v]);
+      out.vslot_off.push_back(sb + P.vslot_off[v + 1]);
+      for (int j = 0; j < 3; ++j) out.xyz_p[(size_t)j * nv + vb + v] = P.xyz_p[(size_t)j * P.nv + v];
+    }
+    for (int p = 0; p < P.nparts; ++p) {
+      out.vert_offsets.push_back(vb + P.vert_offsets[p + 1]);
+      out.ele_offsets.push_back(cb + P.ele_offsets[p + 1]);
+      out.ghost_offsets.push_back(gb + P.ghost_offsets[p + 1]);
+      out.padj_off.push_back(ab + P.padj_off[p + 1]);
+      out.patch_mesh.push_back((int)k);
+    }
+    for (long long c = 0; c < P.full; ++c) out.ele_permute.push_back(eb + P.ele_permute[c]);
+    for (int x : P.conn) out.conn.push_back(vb + x);
+    out.conn_local.insert(out.conn_local.end(), P.conn_local.begin(), P.conn_local.end());
+    for (int g : P.ghost_ids) out.ghost_ids.push_back(vb + g);
+    out.vslot.insert(out.vslot.end(), P.vslot.begin(), P.vslot.end());
+    for (int q : P.padj) out.padj.push_back(pb + q);
+    out.lep = std::max(out.lep, P.lep);
+    out.lvp = std::max(out.lvp, P.lvp);
+    out.lgp = std::max(out.lgp, P.lgp);
+    out.lim = std::max(out.lim, P.lim);
+    out.has_internal_edge = out.has_internal_edge || P.has_internal_edge;
+    out.mesh_edge.push_back(P.mean_edge);
+    vb += P.nv; eb += P.ne; pb += P.nparts; cb += (int)P.full;
+    gb += (int)P.ghost_ids.size(); sb += (int)P.vslot.size(); ab += (int)P.padj.size();
+  }
+  // the union's mean edge (used only where one FIM frame serves all meshes)
+  double w = 0, s = 0;
+  for (const Layout* P : parts) { w += (double)P->ne; s += P->mean_edge * (double)P->ne; }
+  out.mean_edge = w > 0 ? s / w : 1.0;
   return "";
 }
 

@@ -43,11 +43,21 @@ struct Layout {
   bool has_internal_edge = false;
   // permuted coordinates, SoA [3][nv]
   std::vector<float> xyz_p;
+  // batches of independent meshes (merge_layouts): mesh of each patch and
+  // the mean edge length of each mesh; empty for a single mesh
+  std::vector<int> patch_mesh;
+  std::vector<double> mesh_edge;
 };
 
 // Build the layout.  Returns an empty string on success, else the reason.
 std::string build_layout(int dim, int nv, const float* xyz, int ne, const int* elems,
                          const int* npart, int nparts, Layout& L);
+
+// Layout of the disjoint union of independently laid-out meshes: mesh k's
+// vertices, elements, patches and copies follow those of meshes 0..k-1, so
+// the result equals build_layout() on the union mesh with mesh k's patch
+// labels offset by the patch count of the meshes before it.
+std::string merge_layouts(const std::vector<const Layout*>& parts, Layout& out);
 
 // Reference-format arrays (meshFIM3d member arrays) for bit-exact checks.
 enum RefArray {

@@ -84,14 +84,32 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   // solver's polynomial terms are O(1) in FP32 whatever the caller's units.
   const bool ref = cfg.ref_compat != 0;
   const double scale = ref ? 1.0 : (cfg.length_scale > 0 ? cfg.length_scale : L.mean_edge);
+  // batches: each mesh has its own FIM frame
+  const bool batch = !L.patch_mesh.empty();
+  const int nmesh = batch ? (int)L.mesh_edge.size() : 1;
+  std::vector<double> mscale(nmesh, scale);
+  std::vector<double> copy_scale;
+  if (batch) {
+    if ((int)cfg.mesh_dt.size() != nmesh || (int)cfg.mesh_bandwidth.size() != nmesh ||
+        (int)cfg.mesh_curv.size() != nmesh || (int)cfg.mesh_length_scale.size() != nmesh) {
+      status_ = 1;
+      return "per-mesh parameters missing";
+    }
+    for (int k = 0; k < nmesh; ++k)
+      mscale[k] = ref ? 1.0 : (cfg.mesh_length_scale[k] > 0 ? cfg.mesh_length_scale[k] : L.mesh_edge[k]);
+    copy_scale.resize(full);
+    for (int p = 0; p < np; ++p)
+      for (int c = L.ele_offsets[p]; c < L.ele_offsets[p + 1]; ++c) copy_scale[c] = mscale[L.patch_mesh[p]];
+  }
   for (long long c = 0; c < full; ++c) {
+    const double cs = batch ? copy_scale[c] : scale;
     const int e = L.ele_permute[c];
     if (L.dim == 3) {
       float P[4][3], Lc[6];
       for (int k = 0; k < 4; ++k)
         for (int j = 0; j < 3; ++j) P[k][j] = L.xyz_p[(size_t)j * nv + L.conn[c * 4 + k]];
       tet_local_coords(P, Lc);
-      for (int i = 0; i < 6; ++i) lc[i * full + c] = ref ? Lc[i] : (float)((double)Lc[i] / scale);
+      for (int i = 0; i < 6; ++i) lc[i * full + c] = ref ? Lc[i] : (float)((double)Lc[i] / cs);
       if (vel)
         for (int j = 0; j < 3; ++j) sig[j * full + c] = vel[(size_t)e * 3 + j];
     } else {
@@ -101,7 +119,7 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
       if (vel)
         for (int j = 0; j < 3; ++j) vv[j] = vel[(size_t)e * 3 + j];
       tri_local_coords(P, vv, Lc, sg);
-      for (int i = 0; i < 3; ++i) lc[i * full + c] = (float)(ref ? Lc[i] : Lc[i] / scale);
+      for (int i = 0; i < 3; ++i) lc[i * full + c] = (float)(ref ? Lc[i] : Lc[i] / cs);
       sig[c] = (float)sg[0];
       sig[full + c] = (float)sg[1];
     }
@@ -134,6 +152,16 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(upload(A, &m_.xyz, L.xyz_p, stream_), "upload");
   LS_TRY(upload(A, &m_.ipermute, ipermute, stream_), "upload");
   LS_TRY(upload(A, &m_.patch_bytes, pbytes, stream_), "upload");
+  m_.patch_mesh = nullptr;
+  m_.mesh_par = nullptr;
+  if (batch) {
+    std::vector<float4> mp(nmesh);
+    for (int k = 0; k < nmesh; ++k)
+      mp[k] = make_float4((float)(cfg.mesh_bandwidth[k] / mscale[k]), (float)mscale[k], (float)cfg.mesh_dt[k],
+                          (float)cfg.mesh_curv[k]);
+    LS_TRY(upload(A, &m_.patch_mesh, L.patch_mesh, stream_), "upload");
+    LS_TRY(upload(A, &m_.mesh_par, mp, stream_), "upload");
+  }
   // step state
   LS_TRY(dalloc(A, &s_.phi, nv), "alloc");
   LS_TRY(dalloc(A, &s_.phi_out, nv), "alloc");
@@ -465,6 +493,10 @@ std::string Solver::step_host(const float* phi_in, float* phi_out) {
 }
 
 std::string Solver::eikonal(const int* seeds, const float* values, int nseeds, float* out) {
+  if (m_.patch_mesh) {
+    status_ = 1;
+    return "the standalone eikonal solve takes one mesh, not a batch";
+  }
   const Layout& L = *lay_;
   const int nv = m_.nv, np = m_.nparts;
   const float LN = sp_.largenum;

@@ -57,6 +57,9 @@ struct SolverConfig {
   double largenum = 1e9;
   double length_scale = 0.0;
   double fp64_tau = 3.814697265625e-06;  // 2^-18
+  // batches (Layout::patch_mesh set): per-mesh dt, bandwidth, curvature
+  // coefficient and FIM length scale (<= 0: the mesh's mean edge)
+  std::vector<double> mesh_dt, mesh_bandwidth, mesh_curv, mesh_length_scale;
 };
 
 struct SolverStats {

@@ -61,7 +61,10 @@ EXPORTS = [
     "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_narrowband",
     "ls_get_layout_info", "ls_get_layout", "ls_last_error", "ls_version", "ls_partition_structured",
     "ls_partition_rcb", "ls_set_profile", "ls_debug_active", "ls_narrowband_noalloc", "ls_load_mesh",
-    "ls_get_mesh_info", "ls_get_mesh", "ls_write_vtk", "ls_eikonal",
+    "ls_get_mesh_info", "ls_get_mesh", "ls_write_vtk", "ls_eikonal", "ls_batch_create", "ls_batch_destroy",
+    "ls_batch_last_error", "ls_batch_add", "ls_batch_setup", "ls_batch_solve", "ls_batch_get_phi",
+    "ls_batch_get_stats", "ls_batch_reset_stats", "ls_batch_set_profile", "ls_batch_get_layout_info",
+    "ls_batch_get_layout",
 ]
 
 _lib = None
@@ -100,6 +103,19 @@ def lib():
     L.ls_get_mesh.argtypes = [P, V, V]
     L.ls_write_vtk.argtypes = [P, ctypes.c_char_p, V]
     L.ls_eikonal.argtypes = [P, V, V, I, V]
+    L.ls_batch_create.argtypes = [ctypes.POINTER(P)]
+    L.ls_batch_destroy.argtypes = [P]
+    L.ls_batch_last_error.argtypes = [P]
+    L.ls_batch_last_error.restype = ctypes.c_char_p
+    L.ls_batch_add.argtypes = [P, P, ctypes.POINTER(I)]
+    L.ls_batch_setup.argtypes = [P]
+    L.ls_batch_solve.argtypes = [P, I, ctypes.POINTER(I)]
+    L.ls_batch_get_phi.argtypes = [P, I, V]
+    L.ls_batch_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
+    L.ls_batch_reset_stats.argtypes = [P]
+    L.ls_batch_set_profile.argtypes = [P, I]
+    L.ls_batch_get_layout_info.argtypes = [P, V]
+    L.ls_batch_get_layout.argtypes = [P, I, V]
     L.ls_narrowband_noalloc.argtypes = [I, I, V, V, V, ctypes.c_float, ctypes.c_float, ctypes.c_float, V, V, V, V]
     L.ls_get_narrowband.argtypes = [P, V]
     L.ls_get_layout_info.argtypes = [P, V]
@@ -111,7 +127,7 @@ def lib():
     L.ls_partition_rcb.argtypes = [I, V, I, I, V, ctypes.POINTER(I)]
     for name in EXPORTS:
         fn = getattr(L, name)
-        if name not in ("ls_last_error", "ls_version"):
+        if name not in ("ls_last_error", "ls_version", "ls_batch_last_error"):
             fn.restype = ctypes.c_int
     _lib = L
     return L
@@ -287,18 +303,89 @@ class LevelSet:
         return dict(zip(keys, (int(x) for x in info)))
 
     def layout(self, name):
-        info = self.layout_info()
-        d1 = info["dim"] + 1
-        sizes = {
-            "ele_permute": info["full"], "ele_offsets": info["nparts"] + 1, "vert_permute": info["nv"],
-            "vert_ipermute": info["nv"], "vert_offsets": info["nparts"] + 1,
-            "ele_after_permute": d1 * info["full"], "mem_locations": d1 * info["full"],
-            "mem_location_offsets": info["nv"] + 1, "block_xadj": info["nparts"] + 1,
-            "block_adjncy": info["nadj"], "local_coords": (6 if d1 == 4 else 3) * info["full"],
-        }
-        dt = np.float32 if name == "local_coords" else np.int32
-        out = np.zeros(sizes[name], dt)
+        out = _layout_buffer(self.layout_info(), name)
         self._check(lib().ls_get_layout(self._h, REF_ARRAYS[name], _ptr(out)), "layout")
+        return out
+
+
+_LAYOUT_KEYS = ["nparts", "full", "lep", "lvp", "lgp", "lim", "nadj", "nv", "ne", "dim"]
+
+
+def _layout_buffer(info, name):
+    d1 = info["dim"] + 1
+    sizes = {
+        "ele_permute": info["full"], "ele_offsets": info["nparts"] + 1, "vert_permute": info["nv"],
+        "vert_ipermute": info["nv"], "vert_offsets": info["nparts"] + 1,
+        "ele_after_permute": d1 * info["full"], "mem_locations": d1 * info["full"],
+        "mem_location_offsets": info["nv"] + 1, "block_xadj": info["nparts"] + 1,
+        "block_adjncy": info["nadj"], "local_coords": (6 if d1 == 4 else 3) * info["full"],
+    }
+    return np.zeros(sizes[name], np.float32 if name == "local_coords" else np.int32)
+
+
+class LevelSetBatch:
+    """Batch of independent meshes stepped together (ls_batch_*)."""
+
+    def __init__(self):
+        self._b = ctypes.c_void_p()
+        rc = lib().ls_batch_create(ctypes.byref(self._b))
+        if rc:
+            raise LevelSetError(rc, "batch create")
+        self.sizes = []
+
+    def close(self):
+        if self._b:
+            lib().ls_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != LS_OK:
+            raise LevelSetError(rc, "%s: %s" % (what, lib().ls_batch_last_error(self._b).decode()))
+
+    def add(self, ls):
+        idx = ctypes.c_int(-1)
+        self._check(lib().ls_batch_add(self._b, ls._h, ctypes.byref(idx)), "batch add")
+        self.sizes.append(ls.nv)
+        return idx.value
+
+    def setup(self):
+        self._check(lib().ls_batch_setup(self._b), "batch setup")
+
+    def solve(self, nsteps):
+        done = ctypes.c_int(0)
+        self._check(lib().ls_batch_solve(self._b, nsteps, ctypes.byref(done)), "batch solve")
+        return done.value
+
+    def phi(self, index):
+        out = np.zeros(self.sizes[index], np.float32)
+        self._check(lib().ls_batch_get_phi(self._b, index, _ptr(out)), "batch get_phi")
+        return out
+
+    def stats(self):
+        s = Stats()
+        self._check(lib().ls_batch_get_stats(self._b, ctypes.byref(s)), "batch stats")
+        return s.as_dict()
+
+    def reset_stats(self):
+        self._check(lib().ls_batch_reset_stats(self._b), "batch reset_stats")
+
+    def set_profile(self, on):
+        self._check(lib().ls_batch_set_profile(self._b, 1 if on else 0), "batch set_profile")
+
+    def layout_info(self):
+        info = np.zeros(10, np.int64)
+        self._check(lib().ls_batch_get_layout_info(self._b, _ptr(info)), "batch layout_info")
+        return dict(zip(_LAYOUT_KEYS, (int(x) for x in info)))
+
+    def layout(self, name):
+        out = _layout_buffer(self.layout_info(), name)
+        self._check(lib().ls_batch_get_layout(self._b, REF_ARRAYS[name], _ptr(out)), "batch layout")
         return out
 
 

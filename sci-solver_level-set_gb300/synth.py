@@ -168,6 +168,35 @@ def workload(name, seed=0, scale=1.0, n=None):
     return dict(xyz=xyz, elems=el, phi0=phi, vel=vel, npart=npart, nparts=nparts, **cfg)
 
 
+def workload_batch(seed=0, nmesh=64, nmin=16, nmax=64, steps=100):
+    """The batched configuration: nmesh independent jittered unit cubes with
+    cells per side log-uniform in [nmin, nmax], each with a union of 1-3
+    spheres (centres U[0.25, 0.75]^3, radii U(0.1, 0.25)) and a rigid rotation
+    about a random axis (uniform on the sphere) through the cube centre with
+    omega U(1, 6); dt = 0.5 h / max|v| (CFL 0.5), narrowband 5h, 3^3-vertex
+    patches, advection.  Returns a list of workload() dictionaries."""
+    rng = np.random.default_rng(5000 + seed)
+    out = []
+    for k in range(nmesh):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        h = 1.0 / n
+        xyz, el = cube_mesh(n, 0.15, seed=10000 * (seed + 1) + k)
+        ns = int(rng.integers(1, 4))
+        centers = rng.uniform(0.25, 0.75, size=(ns, 3))
+        radii = rng.uniform(0.1, 0.25, size=ns)
+        phi = phi_spheres(xyz, centers, radii)
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        omega = float(rng.uniform(1.0, 6.0))
+        vel = velocity_rotation(xyz, el, omega, axis=axis)
+        vmax = float(np.sqrt((vel.astype(np.float64) ** 2).sum(1)).max())
+        npart, nparts = structured_partition(3, n + 1, 3)
+        out.append(dict(xyz=xyz, elems=el, phi0=phi, vel=vel, npart=npart, nparts=nparts, dim=3, steps=steps,
+                        dt=0.5 * h / vmax, bandwidth=5 * h, update="advect", block=3, name="c5-%d" % k, n=n, h=h,
+                        seed=seed, omega=omega, axis=axis, centers=centers, radii=radii))
+    return out
+
+
 def write_tetgen(base, xyz, tets, first=0):
     """tetgen .node/.ele pair (index base `first`, with a comment line)."""
     xyz = np.asarray(xyz, np.float64)
