@@ -233,6 +233,8 @@ def main():
     ap.add_argument("--fp64-flagged", action="store_true", help="precision form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 0 = library default)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep 3x3x3-vertex patches and the default FIM CTAs per SM instead of the autotuner's pick")
     ap.add_argument("--workload", default="c3", choices=["c3", "c5"],
                     help="c3: the 128^3 curvature-flow benchmark; c5: 64 independent meshes as one batch")
     args = ap.parse_args()
@@ -259,7 +261,26 @@ def main():
         dist = dist_mod
     torch.cuda.set_device(local)
     extra = {"fim_ctas_per_sm": args.ctas} if args.ctas else {}
-    ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged, **extra)
+    tune = None
+    if args.no_autotune:
+        ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged, **extra)
+    else:
+        # structured blocks of a tuned side (the autotuner times 2 steps per
+        # candidate patch size and CTAs-per-SM setting, from phi0)
+        flags = lsgb300.FP64_FLAGGED if args.fp64_flagged else 0
+        p = lsgb300.default_params(time_step=w["dt"], bandwidth=w["bandwidth"], update_kind=lsgb300.UPDATE_CURVATURE,
+                                   curv_coeff=1.0, partition_type=1, side_lengths=w["n"] + 1, block_size=3,
+                                   flags=flags, **extra)
+        ls = lsgb300.LevelSet(False, p)
+        ls.set_mesh(w["xyz"], w["elems"])
+        ls.set_phi(w["phi0"])
+        ls.set_velocity(w["vel"])
+        trials, best = ls.autotune(2)
+        tp = ls.get_params()
+        tune = {"patch_side_vertices": tp.block_size, "fim_ctas_per_sm": tp.fim_ctas_per_sm,
+                "trials": [[t["patch_size"], t["fim_ctas_per_sm"], round(t["ms_per_step"], 3)] for t in trials]}
+        w["label"] = w["label"].replace("3x3x3-vertex patches", "%dx%dx%d-vertex patches (autotuned)" % (
+            (tp.block_size,) * 3))
     nv = len(w["xyz"])
     # L2 flush buffer (larger than the 129 MB L2), written between timed steps
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -357,7 +378,8 @@ def main():
                        "check_visits_per_step": st["check_visits"] / args.steps,
                        "nb_patches_per_step": st["nb_patches"] / args.steps,
                        "flagged_fp64_solves": st["flagged_copies"],
-                       "kernel_ms_per_step_profiled": kernel_ms},
+                       "kernel_ms_per_step_profiled": kernel_ms,
+                       "autotune": tune},
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * nv, "d2h_bytes_per_step": 4 * nv,
                     "steps": e2e_steps},

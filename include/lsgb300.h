@@ -66,7 +66,8 @@ enum {
   LS_FP64_FLAGGED = 1u << 1,
   /* Record per-kernel CUDA-event timings (ls_get_stats). */
   LS_PROFILE = 1u << 2,
-  /* Do not use CUDA graphs for the FIM iteration chunks. */
+  /* Do not run the time step as one CUDA graph (launch kernel by kernel;
+   * the host checks the active list every graph_chunk FIM iterations). */
   LS_NO_GRAPH = 1u << 3,
   /* Use the bit-exact kernel build (no FMA contraction; every float
    * operation individually rounded in the reference's order).  Slower;
@@ -95,7 +96,7 @@ typedef struct ls_params {
   double largenum;        /* 0 -> 1e9  */
   double length_scale;    /* FIM length unit when not LS_REF_COMPAT (0 -> mean edge length) */
   double fp64_threshold;  /* LS_FP64_FLAGGED: discriminant cancellation threshold tau (0 -> 2^-18) */
-  int graph_chunk;        /* FIM iterations per graph launch / host check (0 -> 4) */
+  int graph_chunk;        /* FIM iterations per loop body of the step graph (0 -> 4, rounded up to even) */
   int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 (0 -> 3) */
 } ls_params;
 
@@ -237,6 +238,29 @@ ls_status ls_partition_structured(int dim, int nside, int block, int nv, int* np
  * recursive coordinate bisection into ceil(nv / target) parts (3D) or
  * max(2, nv / target) parts (2D, meshFIM2d.cu:380-382). */
 ls_status ls_partition_rcb(int dim, const float* xyz, int nv, int target, int* npart, int* nparts);
+
+/* Autotuner (no counterpart in the reference): times trial_steps steps (after
+ * one warm-up step, from the handle's phi0) for each candidate patch size --
+ * structured block side 2, 3, 4 (3D) / 4, 5, 6, 8 (2D) when
+ * partition_type = 1, RCB target 8, 16, 27, 32, 64 (3D) / 16, 25, 36, 64
+ * (2D) otherwise, or only the caller's partition when ls_set_partition was
+ * used -- and each FIM CTAs-per-SM setting (2, 3, 4; patches of up to 384
+ * element copies), picks the highest narrowband vertex-updates/s, writes it
+ * into the handle's parameters (block_size or metis_size,
+ * fim_ctas_per_sm) and leaves the handle set up at phi0 with it. */
+#define LS_TUNE_MAX_TRIALS 32
+typedef struct ls_tune_trial {
+  int patch_size;       /* block side or RCB target; 0 = the caller's partition */
+  int fim_ctas_per_sm;
+  double ms_per_step;
+  double updates_per_s;
+} ls_tune_trial;
+typedef struct ls_tune_report {
+  int ntrials;
+  int best;             /* index into trials */
+  ls_tune_trial trials[LS_TUNE_MAX_TRIALS];
+} ls_tune_report;
+ls_status ls_autotune(ls_handle* h, int trial_steps, ls_tune_report* rep);
 
 /* Batches of independent meshes (no counterpart in the reference, which
  * solves one mesh per LevelSet and process).  Each member is a handle with

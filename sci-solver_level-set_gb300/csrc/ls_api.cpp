@@ -23,6 +23,7 @@ struct ls_handle {
   int nv = 0, ne = 0;
   std::vector<int> npart;
   int nparts = 0;
+  bool user_partition = false;  // npart came from ls_set_partition
   std::vector<float> phi;
   std::vector<float> vel;
   bool have_phi = false, have_vel = false;
@@ -209,6 +210,7 @@ ls_status ls_set_mesh(ls_handle* h, const float* xyz, int nv, const int* elems, 
   h->ne = ne;
   h->npart.clear();
   h->nparts = 0;
+  h->user_partition = false;
   h->have_phi = h->have_vel = false;
   h->layout.reset();
   h->solver.reset();
@@ -255,6 +257,7 @@ ls_status ls_set_partition(ls_handle* h, const int* npart, int nparts) {
     if (npart[v] < 0 || npart[v] >= nparts) return fail(h, LS_BAD_INPUT, "partition label out of range");
   h->npart.assign(npart, npart + h->nv);
   h->nparts = nparts;
+  h->user_partition = true;
   h->layout.reset();
   h->solver.reset();
   return LS_OK;
@@ -445,6 +448,85 @@ ls_status ls_debug_active(ls_handle* h, int* list, int cap, int* count, float* d
     for (int i = 0; i < (int)v.size() && i < cap; ++i) list[i] = v[i];
   if (dt) return solver_status(h, h->solver->dt_values(dt));
   return LS_OK;
+}
+
+ls_status ls_autotune(ls_handle* h, int trial_steps, ls_tune_report* rep) {
+  if (!h) return LS_BAD_INPUT;
+  if (h->nv == 0) return fail(h, LS_BAD_INPUT, "You must initialize the mesh first!");
+  if (trial_steps <= 0) trial_steps = 2;
+  // patch-size candidates: structured block side, or RCB target size
+  std::vector<int> sizes;
+  const bool structured = h->prm.partition_type == 1;
+  if (h->user_partition) sizes.push_back(0);
+  else if (structured) sizes = (h->is_tri ? std::vector<int>{4, 5, 6, 8} : std::vector<int>{2, 3, 4});
+  else sizes = (h->is_tri ? std::vector<int>{16, 25, 36, 64} : std::vector<int>{8, 16, 27, 32, 64});
+  const std::vector<int> ctas = {2, 3, 4};
+  const ls_params saved = h->prm;
+  struct Trial { int size, ctas; double ms, rate; };
+  std::vector<Trial> trials;
+  const std::vector<float> phi0 = h->phi;
+  const bool had_phi = h->have_phi;
+  for (int sz : sizes) {
+    if (sz > 0) {
+      if (structured) h->prm.block_size = sz;
+      else h->prm.metis_size = sz;
+      h->npart.clear();
+      h->layout.reset();
+      h->solver.reset();
+    }
+    ls_status s = ls_prepare(h);
+    if (s == LS_PATCH_TOO_LARGE) continue;
+    if (s != LS_OK) { h->prm = saved; return s; }
+    // CTAs per SM only matter for patches of up to 384 element copies
+    const std::vector<int> cs = h->layout->lep <= 384 ? ctas : std::vector<int>{saved.fim_ctas_per_sm};
+    for (int nc : cs) {
+      h->prm.fim_ctas_per_sm = nc;
+      h->prm.flags &= ~(unsigned)LS_PROFILE;
+      s = ls_setup(h);
+      if (s == LS_PATCH_TOO_LARGE) break;
+      if (s != LS_OK) { h->prm = saved; return s; }
+      int done = 0;
+      std::string r = h->solver->run(1, nullptr, &done);  // warm-up (graph upload, caches)
+      if (!r.empty()) { h->prm = saved; return solver_status(h, r); }
+      h->solver->reset_stats();
+      r = h->solver->run(trial_steps, nullptr, &done);
+      if (!r.empty()) { h->prm = saved; return solver_status(h, r); }
+      lsgb::SolverStats t;
+      h->solver->stats(t);
+      const double ms = done > 0 ? t.ms_total / done : 0.0;
+      const double rate = t.ms_total > 0 ? (double)t.nb_vertex_updates / (t.ms_total / 1000.0) : 0.0;
+      trials.push_back({sz, nc, ms, rate});
+      h->phi = phi0;
+      h->have_phi = had_phi;
+    }
+  }
+  if (trials.empty()) { h->prm = saved; return fail(h, LS_PATCH_TOO_LARGE, "no candidate fits"); }
+  int best = 0;
+  for (int i = 1; i < (int)trials.size(); ++i)
+    if (trials[i].rate > trials[best].rate) best = i;
+  // leave the handle set up with the best candidate, phi back at phi0
+  h->prm = saved;
+  if (trials[best].size > 0) {
+    if (structured) h->prm.block_size = trials[best].size;
+    else h->prm.metis_size = trials[best].size;
+    h->npart.clear();
+    h->layout.reset();
+  }
+  h->prm.fim_ctas_per_sm = trials[best].ctas;
+  h->solver.reset();
+  ls_status s = ls_setup(h);
+  if (rep) {
+    std::memset(rep, 0, sizeof(*rep));
+    rep->ntrials = std::min((int)trials.size(), LS_TUNE_MAX_TRIALS);
+    for (int i = 0; i < rep->ntrials; ++i) {
+      rep->trials[i].patch_size = trials[i].size;
+      rep->trials[i].fim_ctas_per_sm = trials[i].ctas;
+      rep->trials[i].ms_per_step = trials[i].ms;
+      rep->trials[i].updates_per_s = trials[i].rate;
+    }
+    rep->best = best;
+  }
+  return s;
 }
 
 ls_status ls_get_layout_info(ls_handle* h, long long* info) {

@@ -64,8 +64,17 @@ EXPORTS = [
     "ls_get_mesh_info", "ls_get_mesh", "ls_write_vtk", "ls_eikonal", "ls_batch_create", "ls_batch_destroy",
     "ls_batch_last_error", "ls_batch_add", "ls_batch_setup", "ls_batch_solve", "ls_batch_get_phi",
     "ls_batch_get_stats", "ls_batch_reset_stats", "ls_batch_set_profile", "ls_batch_get_layout_info",
-    "ls_batch_get_layout",
+    "ls_batch_get_layout", "ls_autotune",
 ]
+
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("patch_size", ctypes.c_int), ("fim_ctas_per_sm", ctypes.c_int), ("ms_per_step", ctypes.c_double),
+                ("updates_per_s", ctypes.c_double)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("ntrials", ctypes.c_int), ("best", ctypes.c_int), ("trials", TuneTrial * 32)]
+
 
 _lib = None
 
@@ -103,6 +112,7 @@ def lib():
     L.ls_get_mesh.argtypes = [P, V, V]
     L.ls_write_vtk.argtypes = [P, ctypes.c_char_p, V]
     L.ls_eikonal.argtypes = [P, V, V, I, V]
+    L.ls_autotune.argtypes = [P, I, ctypes.POINTER(TuneReport)]
     L.ls_batch_create.argtypes = [ctypes.POINTER(P)]
     L.ls_batch_destroy.argtypes = [P]
     L.ls_batch_last_error.argtypes = [P]
@@ -228,6 +238,20 @@ class LevelSet:
         out = np.zeros(self.nv, np.float32)
         self._check(lib().ls_eikonal(self._h, _ptr(s), _ptr(v), len(s), _ptr(out)), "eikonal")
         return out
+
+    def autotune(self, trial_steps=2):
+        """ls_autotune: returns (trials, best index); the handle is left set up
+        with the best patch size and CTAs per SM."""
+        r = TuneReport()
+        self._check(lib().ls_autotune(self._h, int(trial_steps), ctypes.byref(r)), "autotune")
+        trials = [dict(patch_size=t.patch_size, fim_ctas_per_sm=t.fim_ctas_per_sm, ms_per_step=t.ms_per_step,
+                       updates_per_s=t.updates_per_s) for t in r.trials[: r.ntrials]]
+        return trials, r.best
+
+    def get_params(self):
+        p = Params()
+        self._check(lib().ls_get_params(self._h, ctypes.byref(p)), "get_params")
+        return p
 
     def set_partition(self, npart, nparts):
         a = np.ascontiguousarray(npart, np.int32)
