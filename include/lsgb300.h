@@ -294,6 +294,31 @@ ls_status ls_batch_set_profile(ls_batch* b, int on);
 ls_status ls_batch_get_layout_info(ls_batch* b, long long* info);
 ls_status ls_batch_get_layout(ls_batch* b, int which, void* dst);
 
+/* The learned warm start's network (no counterpart in the reference): a
+ * 128-128-128-128-1 ReLU MLP with BF16 weights and activations and FP32
+ * accumulation on the tcgen05 tensor cores, trained on the GPU (forward,
+ * backward and Adam kernels).  Input: 128 features per sample (32 1-ring
+ * slots x (dx, dy, dz, phi) / h, slot 0 the vertex itself); output: the
+ * signed distance / h after the FIM redistance.  Parameters, fp32, in the
+ * order W1 W2 W3 (128 x 128 each, [out][in]), b1 b2 b3 (128 each), w4
+ * (128), b4 (1): ls_mlp_num_params() floats.  Loss 1/(2n) sum (y - t)^2. */
+typedef struct ls_mlp ls_mlp;
+ls_status ls_mlp_create(ls_mlp** m, unsigned long long seed);
+ls_status ls_mlp_destroy(ls_mlp* m);
+const char* ls_mlp_last_error(ls_mlp* m);
+int ls_mlp_num_params(void);
+ls_status ls_mlp_set_params(ls_mlp* m, const float* params);
+ls_status ls_mlp_get_params(ls_mlp* m, float* params);
+/* x: n x 128 floats (rounded to BF16), y: n outputs */
+ls_status ls_mlp_predict(ls_mlp* m, const float* x, int n, float* y);
+/* gradients of the loss over one batch of n samples (all parameters, same
+ * order as the parameters) and the loss */
+ls_status ls_mlp_gradients(ls_mlp* m, const float* x, const float* t, int n, float* grad, float* loss);
+/* Adam (beta 0.9 / 0.999, eps 1e-8) over epochs passes of the n samples in
+ * batches of `batch`; loss = mean batch loss of the last epoch */
+ls_status ls_mlp_train(ls_mlp* m, const float* x, const float* t, int n, int epochs, int batch, float lr,
+                       float* loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,7 @@
 #include "../../include/lsgb300.h"
 #include "ls_layout.h"
 #include "ls_meshio.h"
+#include "ls_mlp.h"
 #include "ls_solver.h"
 
 struct ls_handle {
@@ -708,6 +709,75 @@ ls_status ls_batch_get_layout(ls_batch* b, int which, void* dst) {
   if (s != LS_OK) return s;
   if (!lsgb::ref_array_copy(*b->layout, which, dst)) return bfail(b, LS_BAD_INPUT, "unknown layout array");
   return LS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The learned warm start's network.
+
+}  // extern "C"
+
+struct ls_mlp {
+  lsgb::mlp::Net net;
+  std::string err;
+};
+
+namespace {
+ls_status mfail(ls_mlp* m, const std::string& msg, ls_status s = LS_CUDA_ERROR) {
+  if (msg.empty()) return LS_OK;
+  if (m) m->err = msg;
+  return s;
+}
+}  // namespace
+
+extern "C" {
+
+ls_status ls_mlp_create(ls_mlp** m, unsigned long long seed) {
+  if (!m) return LS_BAD_INPUT;
+  ls_mlp* x = new (std::nothrow) ls_mlp();
+  if (!x) return LS_NO_MEMORY;
+  std::string r = x->net.init(seed);
+  if (!r.empty()) {
+    delete x;
+    *m = nullptr;
+    return LS_CUDA_ERROR;
+  }
+  *m = x;
+  return LS_OK;
+}
+
+ls_status ls_mlp_destroy(ls_mlp* m) {
+  delete m;
+  return LS_OK;
+}
+
+const char* ls_mlp_last_error(ls_mlp* m) { return m ? m->err.c_str() : "null network"; }
+
+int ls_mlp_num_params(void) { return lsgb::mlp::Net::num_params(); }
+
+ls_status ls_mlp_set_params(ls_mlp* m, const float* p) {
+  if (!m || !p) return LS_BAD_INPUT;
+  return mfail(m, m->net.set_params(p));
+}
+
+ls_status ls_mlp_get_params(ls_mlp* m, float* p) {
+  if (!m || !p) return LS_BAD_INPUT;
+  return mfail(m, m->net.get_params(p));
+}
+
+ls_status ls_mlp_predict(ls_mlp* m, const float* x, int n, float* y) {
+  if (!m || n < 0 || (n > 0 && (!x || !y))) return LS_BAD_INPUT;
+  return mfail(m, m->net.predict(x, n, y));
+}
+
+ls_status ls_mlp_gradients(ls_mlp* m, const float* x, const float* t, int n, float* g, float* loss) {
+  if (!m || n <= 0 || !x || !t || !g) return LS_BAD_INPUT;
+  return mfail(m, m->net.gradients(x, t, n, g, loss));
+}
+
+ls_status ls_mlp_train(ls_mlp* m, const float* x, const float* t, int n, int epochs, int batch, float lr,
+                       float* loss) {
+  if (!m || n <= 0 || !x || !t || epochs <= 0 || batch <= 0 || !(lr > 0.f)) return LS_BAD_INPUT;
+  return mfail(m, m->net.train(x, t, n, epochs, batch, lr, loss));
 }
 
 }  // extern "C"

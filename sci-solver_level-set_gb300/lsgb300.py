@@ -64,7 +64,9 @@ EXPORTS = [
     "ls_get_mesh_info", "ls_get_mesh", "ls_write_vtk", "ls_eikonal", "ls_batch_create", "ls_batch_destroy",
     "ls_batch_last_error", "ls_batch_add", "ls_batch_setup", "ls_batch_solve", "ls_batch_get_phi",
     "ls_batch_get_stats", "ls_batch_reset_stats", "ls_batch_set_profile", "ls_batch_get_layout_info",
-    "ls_batch_get_layout", "ls_autotune",
+    "ls_batch_get_layout", "ls_autotune", "ls_mlp_create", "ls_mlp_destroy", "ls_mlp_last_error",
+    "ls_mlp_num_params", "ls_mlp_set_params", "ls_mlp_get_params", "ls_mlp_predict", "ls_mlp_gradients",
+    "ls_mlp_train",
 ]
 
 class TuneTrial(ctypes.Structure):
@@ -113,6 +115,16 @@ def lib():
     L.ls_write_vtk.argtypes = [P, ctypes.c_char_p, V]
     L.ls_eikonal.argtypes = [P, V, V, I, V]
     L.ls_autotune.argtypes = [P, I, ctypes.POINTER(TuneReport)]
+    L.ls_mlp_create.argtypes = [ctypes.POINTER(P), ctypes.c_ulonglong]
+    L.ls_mlp_destroy.argtypes = [P]
+    L.ls_mlp_last_error.argtypes = [P]
+    L.ls_mlp_last_error.restype = ctypes.c_char_p
+    L.ls_mlp_num_params.argtypes = []
+    L.ls_mlp_set_params.argtypes = [P, V]
+    L.ls_mlp_get_params.argtypes = [P, V]
+    L.ls_mlp_predict.argtypes = [P, V, I, V]
+    L.ls_mlp_gradients.argtypes = [P, V, V, I, V, ctypes.POINTER(ctypes.c_float)]
+    L.ls_mlp_train.argtypes = [P, V, V, I, I, I, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
     L.ls_batch_create.argtypes = [ctypes.POINTER(P)]
     L.ls_batch_destroy.argtypes = [P]
     L.ls_batch_last_error.argtypes = [P]
@@ -137,7 +149,7 @@ def lib():
     L.ls_partition_rcb.argtypes = [I, V, I, I, V, ctypes.POINTER(I)]
     for name in EXPORTS:
         fn = getattr(L, name)
-        if name not in ("ls_last_error", "ls_version", "ls_batch_last_error"):
+        if name not in ("ls_last_error", "ls_version", "ls_batch_last_error", "ls_mlp_last_error"):
             fn.restype = ctypes.c_int
     _lib = L
     return L
@@ -429,3 +441,62 @@ def from_workload(w, ref_compat=False, fp64_flagged=False, profile=False, setup=
     if setup:
         ls.setup()
     return ls
+
+
+class MLP:
+    """The learned warm start's network (ls_mlp_*)."""
+
+    def __init__(self, seed=0):
+        self._m = ctypes.c_void_p()
+        rc = lib().ls_mlp_create(ctypes.byref(self._m), int(seed))
+        if rc:
+            raise LevelSetError(rc, "mlp create")
+        self.nparams = lib().ls_mlp_num_params()
+
+    def close(self):
+        if self._m:
+            lib().ls_mlp_destroy(self._m)
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != LS_OK:
+            raise LevelSetError(rc, "%s: %s" % (what, lib().ls_mlp_last_error(self._m).decode()))
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, np.float32)
+        assert a.size == self.nparams
+        self._check(lib().ls_mlp_set_params(self._m, _ptr(a)), "mlp set_params")
+
+    def params(self):
+        out = np.zeros(self.nparams, np.float32)
+        self._check(lib().ls_mlp_get_params(self._m, _ptr(out)), "mlp get_params")
+        return out
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 128)
+        y = np.zeros(len(x), np.float32)
+        self._check(lib().ls_mlp_predict(self._m, _ptr(x), len(x), _ptr(y)), "mlp predict")
+        return y
+
+    def gradients(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 128)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(self.nparams, np.float32)
+        loss = ctypes.c_float(0)
+        self._check(lib().ls_mlp_gradients(self._m, _ptr(x), _ptr(t), len(x), _ptr(g), ctypes.byref(loss)),
+                    "mlp gradients")
+        return g, loss.value
+
+    def train(self, x, t, epochs=1, batch=65536, lr=1e-3):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 128)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = ctypes.c_float(0)
+        self._check(lib().ls_mlp_train(self._m, _ptr(x), _ptr(t), len(x), int(epochs), int(batch), float(lr),
+                                       ctypes.byref(loss)), "mlp train")
+        return loss.value
