@@ -223,6 +223,84 @@ def run_batched(args, rank, world, local):
     return 0
 
 
+def run_learned(args, rank, world, local):
+    """The curvature-flow workload with the learned warm start: training
+    pairs from this project's FIM on seeded 32^3 and 48^3 curvature-flow and
+    torus-advection runs, the network trained on the GPU, then timed steps at
+    --n cells per side with the warm start (margin 0.3 h, whole-patch resets)
+    next to the same steps of the plain path."""
+    import lsgb300
+    import synth
+    import torch
+
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    m = lsgb300.MLP(11)
+    m.reserve_pairs(1 << 23)
+    t0 = time.perf_counter()
+    for name, n, seed in (("c3", 32, 1), ("c3", 48, 2), ("c2", 32, 3), ("c3", 48, 4)):
+        ls = lsgb300.from_workload(synth.workload(name, n=n, seed=seed))
+        ls.learn_collect(m, 16)
+        ls.close()
+    collect_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = m.train_pairs(epochs=20, batch=65536, lr=1e-3, seed=1)
+    train_s = time.perf_counter() - t0
+    w = synth.workload("c3", seed=0, n=args.n)
+    nv = len(w["xyz"])
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def timed(learned):
+        ls = lsgb300.from_workload(w)
+        if learned:
+            ls.set_learned(m, margin=0.3, reset_mode=0)
+        for _ in range(args.warmup):
+            ls.step(1)
+        ls.reset_stats()
+        ms = 0.0
+        phis = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            before = ls.stats()["ms_total"]
+            ls.step(1)
+            ms += ls.stats()["ms_total"] - before
+            phis.append(ls.phi())
+        st = ls.stats()
+        ls.close()
+        return ms, st, np.array(phis)
+
+    ms_l, st_l, ph_l = timed(True)
+    ms_p, st_p, ph_p = timed(False)
+    band = np.abs(ph_p) <= w["bandwidth"]
+    err = np.abs(ph_l - ph_p)[band] / w["h"]
+    value = st_l["nb_vertex_updates"] / (ms_l / 1000.0)
+    plain = st_p["nb_vertex_updates"] / (ms_p / 1000.0)
+    line = {
+        "metric": "narrowband vertex-updates/s (curvature flow with the learned warm start, %d^3 jittered cube)"
+                  % w["n"],
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_l / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (network bf16, fp32 accumulate)", "data": "synthetic (seeded jittered cube, sphere-union SDF)",
+        "config": {"workload": "c4 learned warm start on c3 %d^3 (%d verts)" % (w["n"], nv),
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "training": {"pairs": m.num_pairs(), "collect_s": collect_s, "train_s": train_s,
+                                "last_epoch_loss": loss, "epochs": 20, "batch": 65536},
+                   "warm_vertices": st_l["warm_vertices"], "moved_beyond_1e-3h": st_l["moved_vertices"],
+                   "unsupported_resets": st_l["unsupported_resets"], "support_rounds": st_l["support_rounds"],
+                   "fallbacks_to_plain": st_l["learned_fallbacks"],
+                   "patch_visits": st_l["patch_visits"], "check_visits": st_l["check_visits"]},
+        "plain": {"value": plain, "ms_per_step": ms_p / args.steps, "patch_visits": st_p["patch_visits"],
+                  "check_visits": st_p["check_visits"]},
+        "learned_over_plain": value / plain,
+        "max_abs_diff_vs_plain_h": float(err.max()) if err.size else 0.0,
+        "e2e": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,12 +313,15 @@ def main():
     ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 0 = library default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep 3x3x3-vertex patches and the default FIM CTAs per SM instead of the autotuner's pick")
-    ap.add_argument("--workload", default="c3", choices=["c3", "c5"],
-                    help="c3: the 128^3 curvature-flow benchmark; c5: 64 independent meshes as one batch")
+    ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5"],
+                    help="c3: the 128^3 curvature-flow benchmark; c4: the same with the learned warm start; "
+                         "c5: 64 independent meshes as one batch")
     args = ap.parse_args()
     rank, world, local = env_rank()
     if args.workload == "c5":
         return run_batched(args, rank, world, local)
+    if args.workload == "c4":
+        return run_learned(args, rank, world, local)
 
     import synth
 

@@ -115,6 +115,13 @@ typedef struct ls_stats {
   long long n_sweep, n_check, n_schedule, n_seed, n_narrowband, n_update;
   long long sweep_slab_bytes;   /* algorithmic bytes read+written by sweeps */
   long long kernel_launches;    /* kernels launched (graph kernels included) */
+  /* learned warm start (ls_set_learned) */
+  long long warm_vertices;      /* vertices started from the network's prediction */
+  long long unsupported_resets; /* warm values below their local-solve support, reset */
+  long long support_rounds;     /* support checks run */
+  long long moved_vertices;     /* warm vertices the FIM moved by more than 1e-3 h */
+  long long learned_fallbacks;  /* steps redone as plain FIM after 16 support rounds */
+  long long pairs_collected;    /* training pairs recorded (ls_learn_collect) */
 } ls_stats;
 
 typedef struct ls_handle ls_handle;
@@ -318,6 +325,31 @@ ls_status ls_mlp_gradients(ls_mlp* m, const float* x, const float* t, int n, flo
  * batches of `batch`; loss = mean batch loss of the last epoch */
 ls_status ls_mlp_train(ls_mlp* m, const float* x, const float* t, int n, int epochs, int batch, float lr,
                        float* loss);
+
+/* Training pairs held by the network on the device: (features of a vertex
+ * of the previous step's narrowband patches before the redistance, its
+ * signed distance / h after it).  ls_learn_collect runs nsteps steps of h
+ * (its state advances as with ls_step) recording the pairs of each step
+ * into m's pair buffer (capacity ls_mlp_reserve_pairs, 4 Mi pairs by
+ * default; overflow is dropped).  ls_mlp_train_pairs shuffles the pairs
+ * once and runs Adam over them. */
+ls_status ls_mlp_reserve_pairs(ls_mlp* m, long long capacity);
+ls_status ls_mlp_clear_pairs(ls_mlp* m);
+ls_status ls_mlp_num_pairs(ls_mlp* m, long long* n);
+ls_status ls_mlp_train_pairs(ls_mlp* m, int epochs, int batch, float lr, unsigned long long seed, float* loss);
+ls_status ls_learn_collect(ls_handle* h, ls_mlp* m, int nsteps, int* steps_done);
+/* Learned warm start for the steps of h (m = NULL turns it off): the FIM of
+ * each step starts the previous narrowband's vertices at |prediction| +
+ * margin (units of h, the FIM length unit) instead of LARGENUM, with all
+ * those patches active; afterwards every reached vertex whose value lies
+ * more than support_tol (units of h; 0 -> 5e-4) below all local solves of
+ * its elements is reset to LARGENUM -- with every other non-seed vertex of
+ * its patch (reset_mode 0) or alone (reset_mode 1) -- and the FIM runs
+ * again, until no such vertex is left (at most 16 rounds, then the step's
+ * redistance is redone as plain FIM).  The network is not owned by h and
+ * must outlive its use.  One mesh per handle (not batches); steps run
+ * launch by launch. */
+ls_status ls_set_learned(ls_handle* h, ls_mlp* m, double margin, double support_tol, int reset_mode);
 
 #ifdef __cplusplus
 }

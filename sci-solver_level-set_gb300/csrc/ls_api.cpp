@@ -110,6 +110,12 @@ void fill_stats(const lsgb::SolverStats& t, ls_stats* s) {
   s->n_seed = t.n_seed; s->n_narrowband = t.n_narrowband; s->n_update = t.n_update;
   s->sweep_slab_bytes = t.sweep_slab_bytes;
   s->kernel_launches = t.kernel_launches;
+  s->warm_vertices = t.warm_vertices;
+  s->unsupported_resets = t.unsupported_resets;
+  s->support_rounds = t.support_rounds;
+  s->moved_vertices = t.moved_vertices;
+  s->learned_fallbacks = t.learned_fallbacks;
+  s->pairs_collected = t.pairs_collected;
 }
 
 // Solver configuration from a handle's parameters.
@@ -778,6 +784,44 @@ ls_status ls_mlp_train(ls_mlp* m, const float* x, const float* t, int n, int epo
                        float* loss) {
   if (!m || n <= 0 || !x || !t || epochs <= 0 || batch <= 0 || !(lr > 0.f)) return LS_BAD_INPUT;
   return mfail(m, m->net.train(x, t, n, epochs, batch, lr, loss));
+}
+
+ls_status ls_mlp_reserve_pairs(ls_mlp* m, long long capacity) {
+  if (!m || capacity <= 0) return LS_BAD_INPUT;
+  return mfail(m, m->net.reserve_pairs(capacity), LS_NO_MEMORY);
+}
+
+ls_status ls_mlp_clear_pairs(ls_mlp* m) {
+  if (!m) return LS_BAD_INPUT;
+  return mfail(m, m->net.clear_pairs());
+}
+
+ls_status ls_mlp_num_pairs(ls_mlp* m, long long* n) {
+  if (!m || !n) return LS_BAD_INPUT;
+  *n = m->net.num_pairs();
+  return LS_OK;
+}
+
+ls_status ls_mlp_train_pairs(ls_mlp* m, int epochs, int batch, float lr, unsigned long long seed, float* loss) {
+  if (!m || epochs <= 0 || batch <= 0 || !(lr > 0.f)) return LS_BAD_INPUT;
+  return mfail(m, m->net.train_pairs(epochs, batch, lr, seed, loss));
+}
+
+ls_status ls_learn_collect(ls_handle* h, ls_mlp* m, int nsteps, int* steps_done) {
+  if (!h || !m || nsteps < 0) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  std::string r = h->solver->set_collect(&m->net);
+  if (!r.empty()) return solver_status(h, r);
+  r = h->solver->run(nsteps, nullptr, steps_done);
+  h->solver->set_collect(nullptr);
+  return solver_status(h, r);
+}
+
+ls_status ls_set_learned(ls_handle* h, ls_mlp* m, double margin, double support_tol, int reset_mode) {
+  if (!h || margin < 0 || support_tol < 0 || reset_mode < 0 || reset_mode > 1) return LS_BAD_INPUT;
+  if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
+  return solver_status(h, h->solver->set_learned(m ? &m->net : nullptr, (float)margin, (float)support_tol,
+                                                 reset_mode == 0));
 }
 
 }  // extern "C"

@@ -69,6 +69,16 @@ struct DevState {
                     // [2] previous narrowband valid (seed search restricted to it)
 };
 
+// Learned warm start / training-pair collection buffers (null when off).
+struct DevLearn {
+  int* vlist;     // warm-set vertices (owned vertices of the previous narrowband patches)
+  int* cnt;       // [0] warm-set size, [1] unsupported vertices reset, [2] vertices moved beyond
+                  // the tolerance, [3] patches re-activated by the support check
+  float* pred;    // network output per warm-set vertex (signed distance / h)
+  float* warm;    // per vertex: warm-start value in the FIM frame
+  float* target;  // collection: signed distance / h after the redistance, per warm-set vertex
+};
+
 struct StepParams {
   float largenum;
   float bandwidth;   // in the FIM frame (divided by scale)

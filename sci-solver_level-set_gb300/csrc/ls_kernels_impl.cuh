@@ -44,7 +44,7 @@ __global__ void k_reset(DevState s, int nv, float LN) {
 // vertex values include an exact zero or differ in sign marks those
 // vertices as seeds with DT = |phi|; the patch joins list0.
 template <int D1>
-__global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
+__global__ void k_seed(DevMesh m, DevState s, int use_all, float scale, int warm) {
   // use_all < 0: decided on the device from the step-control flag
   if (use_all < 0) use_all = s.ctl[2] ? 0 : 1;
   const int count = use_all ? m.nparts : s.counts[3];
@@ -79,7 +79,7 @@ __global__ void k_seed(DevMesh m, DevState s, int use_all, float scale) {
       }
     }
     found = __syncthreads_or(found);
-    if (threadIdx.x == 0 && found) {
+    if (threadIdx.x == 0 && (found || warm)) {
       const int pos = atomicAdd(&s.counts[0], 1);
       s.list0[pos] = p;
     }
@@ -660,14 +660,193 @@ __global__ void k_permute(DevMesh m, const float* in, float* out) {
 
 // ---------------------------------------------------------------------------
 // Launchers (host side).
+// ---------------------------------------------------------------------------
+// Learned warm start.
+
+// Raw local-solve candidates of one copy (no minimum with the vertex's own
+// value): the support of each of its vertices.
+template <int D1, bool XDIV>
+__device__ __forceinline__ void solve_copy_raw(const float* Mt, const float T[4], float out[4], float eps_h,
+                                               double eps_h64, float LN) {
+  if (D1 == 4) {
+    const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4];
+    const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
+    const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
+    bool ill = false;
+    out[3] = tet_solve<float, XDIV, false>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, 0.f, ill);
+    out[0] = tet_solve<float, XDIV, false>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, 0.f, ill);
+    out[1] = tet_solve<float, XDIV, false>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, 0.f, ill);
+    out[2] = tet_solve<float, XDIV, false>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, 0.f, ill);
+  } else {
+    const float LenAB = Mt[0], LenBC = Mt[1], LenCA = Mt[2];
+    const float TA = T[0], TB = T[1], TC = T[2];
+    out[2] = tri_solve<float>(TA, TB, LenAB, LenBC, LenCA, LN);
+    out[0] = tri_solve<float>(TB, TC, LenBC, LenCA, LenAB, LN);
+    out[1] = tri_solve<float>(TC, TA, LenCA, LenAB, LenBC, LN);
+    out[3] = LN;
+  }
+}
+
+// Owned vertices of the patches nblist[0, nb) -> lr.vlist (warp per patch).
+__global__ void k_nb_vertices(DevMesh m, DevState s, DevLearn lr, int nb) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int w = warp_id_global(); w < nb; w += nwarps) {
+    const int p = s.nblist[w];
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&lr.cnt[0], nvp);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (int i = lane; i < nvp; i += 32) lr.vlist[base + i] = vs + i;
+  }
+}
+
+// DT := |prediction| + margin on the warm set (FIM frame, unit h); the seed
+// search that follows overwrites the seeds.
+__global__ void k_warm_apply(DevState s, DevLearn lr, float LN, float margin) {
+  const int n = lr.cnt[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int v = lr.vlist[i];
+    const float w = fminf(fabsf(lr.pred[i]) + margin, LN);
+    s.DT[v] = w;
+    lr.warm[v] = w;
+  }
+}
+
+// Support check after the FIM from a warm start: an owned non-seed vertex
+// whose value lies more than tol below every local solve of its elements
+// (its support) was set by the warm start, not by the wavefront; it is
+// reset to LARGENUM and its patch joins list0 for another FIM loop.  One
+// CTA per patch over all patches; patches without a reached vertex skip.
+template <int D1, bool XDIV>
+__global__ void __launch_bounds__(384) k_support(DevMesh m, DevState s, StepParams sp, DevLearn lr, float tol,
+                                                 int whole_patch) {
+  extern __shared__ float smem[];
+  float* sT = smem;
+  float* sC = smem + sp.lvp + sp.lgp;  // owned candidates
+  const int tid = threadIdx.x;
+  for (int p = blockIdx.x; p < m.nparts; p += gridDim.x) {
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
+    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+    int reached = 0;
+    for (int i = tid; i < nvp + ngp; i += blockDim.x) {
+      const float d = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
+      sT[i] = d;
+      if (i < nvp) {
+        sC[i] = __int_as_float(0x7f800000);
+        reached |= (d < sp.largenum) ? 1 : 0;
+      }
+    }
+    reached = __syncthreads_or(reached);
+    if (!reached) continue;
+    for (int c = tid; c < nep; c += blockDim.x) {
+      const ushort4 cv = m.conn[es + c];
+      const int idx[4] = {cv.x, cv.y, cv.z, cv.w};
+      float T[4] = {0.f, 0.f, 0.f, sp.largenum}, Mt[11], r[4];
+#pragma unroll
+      for (int k = 0; k < D1; ++k) T[k] = sT[idx[k]];
+      copy_metric<D1>(m, (long long)es + c, Mt);
+      solve_copy_raw<D1, XDIV>(Mt, T, r, sp.eps_h, sp.eps_h64, sp.largenum);
+#pragma unroll
+      for (int k = 0; k < D1; ++k)
+        if (idx[k] < nvp) atomicMin(reinterpret_cast<int*>(&sC[idx[k]]), __float_as_int(fmaxf(r[k], 0.f)));
+    }
+    __syncthreads();
+    int bad = 0;
+    for (int i = tid; i < nvp; i += blockDim.x) {
+      const int v = vs + i;
+      if (!s.seed[v] && sT[i] < sp.largenum && sT[i] < sC[i] - tol) {
+        s.DT[v] = sp.largenum;
+        bad++;
+      }
+    }
+    bad = __syncthreads_count(bad);
+    if (bad && whole_patch) {
+      // reset every non-seed vertex of the patch: values that leaned on the
+      // unsupported ones are recomputed in the same FIM loop
+      for (int i = tid; i < nvp; i += blockDim.x)
+        if (!s.seed[vs + i]) s.DT[vs + i] = sp.largenum;
+    }
+    if (tid == 0 && bad) {
+      atomicAdd(&lr.cnt[1], bad);
+      if (atomicCAS(&s.blabel[p], LS_FAR, LS_ACTIVE) == LS_FAR) {
+        const int pos = atomicAdd(&s.counts[0], 1);
+        s.list0[pos] = p;
+        atomicAdd(&lr.cnt[3], 1);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Warm-set vertices whose final value differs from the warm start by more
+// than tol (FIM frame).
+__global__ void k_moved(DevState s, DevLearn lr, float tol) {
+  const int n = lr.cnt[0];
+  int moved = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int v = lr.vlist[i];
+    moved += (fabsf(s.DT[v] - lr.warm[v]) > tol) ? 1 : 0;
+  }
+  moved = __reduce_add_sync(0xffffffffu, moved);
+  if ((threadIdx.x & 31) == 0 && moved) atomicAdd(&lr.cnt[2], moved);
+}
+
+// Collection: signed phi after the redistance, in units of h, per warm-set
+// vertex (NaN where the wavefront did not reach).
+__global__ void k_targets(DevState s, DevLearn lr, float inv_h, float LN) {
+  const int n = lr.cnt[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float ph = s.phi[lr.vlist[i]];
+    lr.target[i] = fabsf(ph) >= LN ? __int_as_float(0x7fc00000) : ph * inv_h;
+  }
+}
+
+cudaError_t launch_learn(int op, const DevMesh& m, const DevState& s, const StepParams& sp, const DevLearn& lr,
+                         int arg, float fa, const Launch& L, cudaStream_t st) {
+  switch (op) {
+    case LEARN_NB_VERTICES:
+      k_nb_vertices<<<L.warp_grid, 256, 0, st>>>(m, s, lr, arg);
+      break;
+    case LEARN_WARM:
+      k_warm_apply<<<L.flat_grid, 256, 0, st>>>(s, lr, sp.largenum, fa);
+      break;
+    case LEARN_SEED_WARM:
+      if (m.dim == 3) k_seed<4><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, 0, sp.scale, 1);
+      else k_seed<3><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, 0, sp.scale, 1);
+      break;
+    case LEARN_SUPPORT: {
+      const int smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
+      const int grid = L.sms * 4;
+      if (m.dim == 3) {
+        if (sp.xdiv) k_support<4, true><<<grid, 384, smem, st>>>(m, s, sp, lr, fa, arg);
+        else k_support<4, false><<<grid, 384, smem, st>>>(m, s, sp, lr, fa, arg);
+      } else {
+        k_support<3, false><<<grid, 384, smem, st>>>(m, s, sp, lr, fa, arg);
+      }
+      break;
+    }
+    case LEARN_MOVED:
+      k_moved<<<L.flat_grid, 256, 0, st>>>(s, lr, fa);
+      break;
+    case LEARN_TARGETS:
+      k_targets<<<L.flat_grid, 256, 0, st>>>(s, lr, fa, sp.largenum);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_reset(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st) {
   k_reset<<<L.flat_grid, 256, 0, st>>>(s, m.nv, sp.largenum);
   return cudaGetLastError();
 }
 
 cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float scale, const Launch& L, cudaStream_t st) {
-  if (m.dim == 3) k_seed<4><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, use_all, scale);
-  else k_seed<3><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, use_all, scale);
+  if (m.dim == 3) k_seed<4><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, use_all, scale, 0);
+  else k_seed<3><<<L.seed_grid, L.fim_block, 0, st>>>(m, s, use_all, scale, 0);
   return cudaGetLastError();
 }
 
@@ -793,7 +972,7 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
 
 
 const KernelSet& kernel_table() {
-  static const KernelSet t = {configure_launch, launch_reset, launch_seed, launch_sweep, launch_schedule,
-                              launch_narrowband, launch_update, launch_unpermute, launch_permute};
+  static const KernelSet t = {configure_launch, launch_reset, launch_seed,    launch_sweep, launch_schedule,
+                              launch_narrowband, launch_update, launch_unpermute, launch_permute, launch_learn};
   return t;
 }

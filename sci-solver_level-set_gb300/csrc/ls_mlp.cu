@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -498,6 +499,39 @@ __global__ void k_features(int nlist, const int* __restrict__ vlist, const int* 
   }
 }
 
+// Training pairs: rows i < *n of X / t with a finite target are appended to
+// the pair buffer (capacity cap; overflow is counted, not written).
+__global__ void k_append_pairs(const __nv_bfloat16* __restrict__ X, const float* __restrict__ t, const int* n_dev,
+                               __nv_bfloat16* __restrict__ PX, float* __restrict__ PT,
+                               unsigned long long* count, long long cap) {
+  const int n = *n_dev;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float v = t[i];
+    if (!isfinite(v)) continue;
+    const unsigned long long pos = atomicAdd(count, 1ull);
+    if ((long long)pos >= cap) continue;
+    const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)i * F);
+    uint4* dst = reinterpret_cast<uint4*>(PX + (size_t)pos * F);
+#pragma unroll 4
+    for (int j = 0; j < F / 8; ++j) dst[j] = src[j];
+    PT[pos] = v;
+  }
+}
+
+// rows perm[i] of (X, t) -> row i of (Xo, to)
+__global__ void k_gather_pairs(const __nv_bfloat16* __restrict__ X, const float* __restrict__ t,
+                               const int* __restrict__ perm, long long n, __nv_bfloat16* __restrict__ Xo,
+                               float* __restrict__ to) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long j = perm[i];
+    const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)j * F);
+    uint4* dst = reinterpret_cast<uint4*>(Xo + (size_t)i * F);
+#pragma unroll 4
+    for (int q = 0; q < F / 8; ++q) dst[q] = src[q];
+    to[i] = t[j];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host side.
 
@@ -516,6 +550,9 @@ size_t bwd_smem() { return 4 * (size_t)TILE_BYTES + F * sizeof(float) + 1024 + 6
 
 Net::~Net() {
   for (void* p : allocs_) cudaFree(p);
+  if (PX_) cudaFree(PX_);
+  if (PT_) cudaFree(PT_);
+  if (pair_count_) cudaFree(pair_count_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -718,6 +755,108 @@ std::string Net::train_device(const __nv_bfloat16* X, const float* t, int n, int
   }
   if (last_loss) *last_loss = loss_cnt ? (float)(loss_sum / loss_cnt) : 0.f;
   return check_err();
+}
+
+std::string Net::reserve_pairs(long long cap) {
+  if (cap <= pair_cap_) return "";
+  __nv_bfloat16* px = nullptr;
+  float* pt = nullptr;
+  MLP_TRY(cudaMalloc(&px, sizeof(__nv_bfloat16) * (size_t)cap * F), "alloc pairs");
+  cudaError_t e = cudaMalloc(&pt, sizeof(float) * (size_t)cap);
+  if (e != cudaSuccess) {
+    cudaFree(px);
+    return std::string("alloc pairs: ") + cudaGetErrorString(e);
+  }
+  if (!pair_count_) MLP_TRY(cudaMalloc(&pair_count_, sizeof(unsigned long long)), "alloc");
+  long long have = 0;
+  if (PX_) {
+    have = num_pairs();
+    if (have > 0) {
+      cudaMemcpyAsync(px, PX_, sizeof(__nv_bfloat16) * (size_t)have * F, cudaMemcpyDeviceToDevice, stream_);
+      cudaMemcpyAsync(pt, PT_, sizeof(float) * (size_t)have, cudaMemcpyDeviceToDevice, stream_);
+    }
+    cudaStreamSynchronize(stream_);
+    cudaFree(PX_);
+    cudaFree(PT_);
+  }
+  PX_ = px;
+  PT_ = pt;
+  pair_cap_ = cap;
+  unsigned long long h = (unsigned long long)have;
+  MLP_TRY(cudaMemcpyAsync(pair_count_, &h, sizeof(h), cudaMemcpyHostToDevice, stream_), "h2d");
+  MLP_TRY(cudaStreamSynchronize(stream_), "sync");
+  return "";
+}
+
+long long Net::num_pairs() {
+  if (!pair_count_) return 0;
+  unsigned long long h = 0;
+  cudaMemcpyAsync(&h, pair_count_, sizeof(h), cudaMemcpyDeviceToHost, stream_);
+  cudaStreamSynchronize(stream_);
+  return (long long)(h < (unsigned long long)pair_cap_ ? h : (unsigned long long)pair_cap_);
+}
+
+std::string Net::clear_pairs() {
+  if (pair_count_) MLP_TRY(cudaMemsetAsync(pair_count_, 0, sizeof(unsigned long long), stream_), "memset");
+  MLP_TRY(cudaStreamSynchronize(stream_), "sync");
+  return "";
+}
+
+std::string Net::append_pairs(const __nv_bfloat16* X, const float* t, const int* n_dev, int max_n, cudaStream_t st,
+                              long long* added) {
+  if (added) *added = 0;
+  if (!PX_) {
+    std::string r = reserve_pairs(1LL << 22);
+    if (!r.empty()) return r;
+  }
+  const long long before = num_pairs();
+  // the solver's stream produced X and t: order this stream after it
+  cudaEvent_t ev;
+  MLP_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+  cudaEventRecord(ev, st);
+  cudaStreamWaitEvent(stream_, ev, 0);
+  cudaEventDestroy(ev);
+  const int grid = (max_n + 255) / 256 < 4096 ? (max_n + 255) / 256 : 4096;
+  k_append_pairs<<<grid > 0 ? grid : 1, 256, 0, stream_>>>(X, t, n_dev, PX_, PT_, pair_count_, pair_cap_);
+  MLP_TRY(cudaGetLastError(), "append pairs");
+  MLP_TRY(cudaStreamSynchronize(stream_), "sync");
+  if (added) *added = num_pairs() - before;
+  return "";
+}
+
+std::string Net::train_pairs(int epochs, int batch, float lr, unsigned long long seed, float* last_loss) {
+  const long long n = num_pairs();
+  if (n <= 0) return "no training pairs";
+  if (n > 0x7fffffffLL) return "too many pairs";
+  // one shuffle of the pairs, then epochs of sequential batches
+  std::vector<int> perm((size_t)n);
+  for (long long i = 0; i < n; ++i) perm[(size_t)i] = (int)i;
+  std::mt19937_64 rng(seed);
+  std::shuffle(perm.begin(), perm.end(), rng);
+  std::vector<void*> tmp;
+  auto fin = [&](const std::string& r) {
+    cudaStreamSynchronize(stream_);
+    for (void* p : tmp) cudaFree(p);
+    return r;
+  };
+  int* dperm = nullptr;
+  __nv_bfloat16 *Xs = nullptr, *Aa = nullptr;
+  float *ts = nullptr, *y = nullptr;
+  const int bmax = (long long)batch < n ? batch : (int)n;
+  if (cudaMalloc(&dperm, sizeof(int) * (size_t)n) != cudaSuccess) return fin("alloc");
+  tmp.push_back(dperm);
+  if (cudaMalloc(&Xs, sizeof(__nv_bfloat16) * (size_t)n * F) != cudaSuccess) return fin("alloc");
+  tmp.push_back(Xs);
+  if (cudaMalloc(&ts, sizeof(float) * (size_t)n) != cudaSuccess) return fin("alloc");
+  tmp.push_back(ts);
+  if (cudaMalloc(&Aa, sizeof(__nv_bfloat16) * 3 * (size_t)bmax * F) != cudaSuccess) return fin("alloc");
+  tmp.push_back(Aa);
+  if (cudaMalloc(&y, sizeof(float) * bmax) != cudaSuccess) return fin("alloc");
+  tmp.push_back(y);
+  cudaMemcpyAsync(dperm, perm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, stream_);
+  k_gather_pairs<<<4096, 256, 0, stream_>>>(PX_, PT_, dperm, n, Xs, ts);
+  if (cudaGetLastError() != cudaSuccess) return fin("gather pairs");
+  return fin(train_device(Xs, ts, (int)n, epochs, batch, lr, Aa, y, last_loss));
 }
 
 }  // namespace mlp

@@ -36,6 +36,13 @@ class Net {
   std::string train_device(const __nv_bfloat16* X, const float* t, int n, int epochs, int batch, float lr,
                            __nv_bfloat16* acts, float* y, float* last_loss);
   std::string check_err();
+  // training pairs (device buffer owned by the network)
+  std::string reserve_pairs(long long cap);
+  std::string clear_pairs();
+  long long num_pairs();
+  std::string append_pairs(const __nv_bfloat16* X, const float* t, const int* n_dev, int max_n, cudaStream_t st,
+                           long long* added);
+  std::string train_pairs(int epochs, int batch, float lr, unsigned long long seed, float* last_loss);
 
  private:
   cudaStream_t stream_ = nullptr;
@@ -44,6 +51,10 @@ class Net {
   __nv_bfloat16 *Wb_ = nullptr, *WTb_ = nullptr;
   int* err_ = nullptr;
   long long step_ = 0;
+  __nv_bfloat16* PX_ = nullptr;
+  float* PT_ = nullptr;
+  unsigned long long* pair_count_ = nullptr;
+  long long pair_cap_ = 0;
 };
 
 }  // namespace mlp

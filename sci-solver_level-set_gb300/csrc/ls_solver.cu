@@ -6,6 +6,7 @@
 // convergence flags stay on the device; the host only launches a fixed
 // chunk of FIM iterations (captured once as a CUDA graph) and reads one
 // counter per chunk to learn whether the active list has drained.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -368,6 +369,7 @@ std::string Solver::one_step(bool* empty_nb) {
     prof_pending().push_back(pe);
     return e;
   };
+  if (net_ || collect_) return learned_step(empty_nb);
   if (graph_exec_ && !cfg_.profile) {
     LS_TRY(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
     LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
@@ -409,6 +411,178 @@ std::string Solver::one_step(bool* empty_nb) {
     for (int it = 0; it < cfg_.inside_niter; ++it) {
       LS_TRY(prof(5, [&] { return K_->update(m_, s_, sp_, L_, stream_); }), "update");
       st_.kernel_launches += 2;  // update, copy-back
+    }
+  }
+  return "";
+}
+
+// ---------------------------------------------------------------------------
+// Learned warm start.
+
+std::string Solver::learn_buffers() {
+  if (X_) return "";
+  if (m_.patch_mesh) {
+    status_ = 1;
+    return "the learned warm start takes one mesh, not a batch";
+  }
+  const Layout& L = *lay_;
+  const int nv = m_.nv, d1 = m_.dim + 1;
+  // 1-ring from the element copies (each element once), sorted and unique
+  std::vector<std::vector<int>> ring(nv);
+  std::vector<char> seen(L.ne, 0);
+  for (long long c = 0; c < L.full; ++c) {
+    const int e = L.ele_permute[c];
+    if (seen[e]) continue;
+    seen[e] = 1;
+    for (int a = 0; a < d1; ++a)
+      for (int b = 0; b < d1; ++b)
+        if (a != b) ring[L.conn[c * d1 + a]].push_back(L.conn[c * d1 + b]);
+  }
+  std::vector<int> off(nv + 1, 0), adj;
+  for (int v = 0; v < nv; ++v) {
+    auto& r = ring[v];
+    std::sort(r.begin(), r.end());
+    r.erase(std::unique(r.begin(), r.end()), r.end());
+    off[v + 1] = off[v] + (int)r.size();
+  }
+  adj.reserve(off[nv]);
+  for (int v = 0; v < nv; ++v) adj.insert(adj.end(), ring[v].begin(), ring[v].end());
+  std::vector<void*>& A = allocs_;
+  const int* d_off = nullptr;
+  const int* d_adj = nullptr;
+  LS_TRY(upload(A, &d_off, off, stream_), "upload");
+  LS_TRY(upload(A, &d_adj, adj, stream_), "upload");
+  adj_off_ = const_cast<int*>(d_off);
+  adj_ = const_cast<int*>(d_adj);
+  LS_TRY(dalloc(A, &lr_.vlist, nv), "alloc");
+  LS_TRY(dalloc(A, &lr_.cnt, 4), "alloc");
+  LS_TRY(dalloc(A, &lr_.pred, nv), "alloc");
+  LS_TRY(dalloc(A, &lr_.warm, nv), "alloc");
+  LS_TRY(dalloc(A, &lr_.target, nv), "alloc");
+  LS_TRY(dalloc(A, &X_, (size_t)nv * 128), "alloc");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  return "";
+}
+
+std::string Solver::set_learned(mlp::Net* net, float margin, float tol, bool whole_patch) {
+  support_patch_ = whole_patch;
+  if (net) {
+    std::string r = learn_buffers();
+    if (!r.empty()) return r;
+  }
+  net_ = net;
+  margin_ = margin;
+  if (tol > 0.f) support_tol_ = tol;
+  return "";
+}
+
+std::string Solver::set_collect(mlp::Net* net) {
+  if (net) {
+    std::string r = learn_buffers();
+    if (!r.empty()) return r;
+  }
+  collect_ = net;
+  return "";
+}
+
+// One time step with the warm start and / or pair collection, launch by
+// launch (the support rounds are decided on the host).
+std::string Solver::learned_step(bool* empty_nb) {
+  *empty_nb = false;
+  const bool prev = have_nb_;
+  const bool warm = net_ && prev;
+  int nb_prev = 0;
+  LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_), "memset");
+  LS_TRY(K_->reset(m_, s_, sp_, L_, stream_), "reset");
+  if (prev) {
+    LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaStreamSynchronize(stream_), "sync");
+    nb_prev = h_counts_[3];
+    LS_TRY(cudaMemsetAsync(lr_.cnt, 0, sizeof(int) * 4, stream_), "memset");
+    LS_TRY(K_->learn(LEARN_NB_VERTICES, m_, s_, sp_, lr_, nb_prev, 0.f, L_, stream_), "warm set");
+    mlp::k_features<<<L_.flat_grid, 256, 0, stream_>>>(0, lr_.vlist, lr_.cnt, adj_off_, adj_, m_.xyz, m_.nv, s_.phi,
+                                                        1.f / sp_.scale, X_);
+    LS_TRY(cudaGetLastError(), "features");
+    st_.kernel_launches += 2;
+    if (warm) {
+      std::string r = net_->forward_dev(X_, 0, lr_.cnt, m_.nv, lr_.pred, nullptr, stream_);
+      if (!r.empty()) return r;
+      LS_TRY(K_->learn(LEARN_WARM, m_, s_, sp_, lr_, 0, margin_, L_, stream_), "warm apply");
+      st_.kernel_launches += 2;
+    }
+  }
+  LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_), "memset");
+  if (warm) LS_TRY(K_->learn(LEARN_SEED_WARM, m_, s_, sp_, lr_, 0, 0.f, L_, stream_), "seed");
+  else LS_TRY(K_->seed(m_, s_, prev ? 0 : 1, sp_.scale, L_, stream_), "seed");
+  LS_TRY(cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_), "memset");
+  st_.kernel_launches += 2;
+  std::string r = fim_loop(sp_);
+  if (!r.empty()) return r;
+  if (warm) {
+    // support rounds: reset unsupported warm values, FIM again, until none
+    const int max_rounds = 16;
+    bool clean = false;
+    for (int round = 0; round < max_rounds; ++round) {
+      LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
+      LS_TRY(K_->learn(LEARN_SUPPORT, m_, s_, sp_, lr_, support_patch_ ? 1 : 0, support_tol_, L_, stream_),
+             "support");
+      LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+      LS_TRY(cudaStreamSynchronize(stream_), "sync");
+      st_.kernel_launches += 1;
+      st_.support_rounds++;
+      if (h_counts_[0] == 0) {
+        clean = true;
+        break;
+      }
+      r = fim_loop(sp_);
+      if (!r.empty()) return r;
+    }
+    if (!clean) {
+      // plain FIM from the seeds: the fallback
+      st_.learned_fallbacks++;
+      LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
+      LS_TRY(cudaMemcpyAsync(s_.counts + 3, &nb_prev, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d");
+      LS_TRY(K_->reset(m_, s_, sp_, L_, stream_), "reset");
+      LS_TRY(cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_), "memset");
+      LS_TRY(K_->seed(m_, s_, 0, sp_.scale, L_, stream_), "seed");
+      LS_TRY(cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_), "memset");
+      r = fim_loop(sp_);
+      if (!r.empty()) return r;
+    }
+    LS_TRY(K_->learn(LEARN_MOVED, m_, s_, sp_, lr_, 0, 1e-3f, L_, stream_), "moved");
+    st_.kernel_launches += 1;
+  }
+  LS_TRY(K_->narrowband(m_, s_, sp_, L_, stream_), "narrowband");
+  k_step_tail<<<1, 32, 0, stream_>>>(s_.counts, s_.ctl);
+  LS_TRY(cudaGetLastError(), "step tail");
+  st_.kernel_launches += 2;
+  if (collect_ && prev) {
+    LS_TRY(K_->learn(LEARN_TARGETS, m_, s_, sp_, lr_, 0, 1.f / sp_.scale, L_, stream_), "targets");
+    st_.kernel_launches += 1;
+    long long added = 0;
+    r = collect_->append_pairs(X_, lr_.target, lr_.cnt, m_.nv, stream_, &added);
+    if (!r.empty()) return r;
+    st_.pairs_collected += added;
+  }
+  LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaMemcpyAsync(h_counts_ + 8, lr_.cnt, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream_), "d2h");
+  LS_TRY(cudaStreamSynchronize(stream_), "sync");
+  if (warm) {
+    st_.warm_vertices += h_counts_[8];
+    st_.unsupported_resets += h_counts_[9];
+    st_.moved_vertices += h_counts_[10];
+  }
+  if (h_counts_[3] == 0) {
+    *empty_nb = true;
+    have_nb_ = false;
+    return "";
+  }
+  have_nb_ = true;
+  if (cfg_.update_kind != 2) {
+    for (int it = 0; it < cfg_.inside_niter; ++it) {
+      LS_TRY(K_->update(m_, s_, sp_, L_, stream_), "update");
+      st_.kernel_launches += 2;
     }
   }
   return "";

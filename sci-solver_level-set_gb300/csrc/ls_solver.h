@@ -8,6 +8,7 @@
 
 #include "ls_device.cuh"
 #include "ls_layout.h"
+#include "ls_mlp.h"
 
 namespace lsgb {
 
@@ -19,6 +20,8 @@ struct Launch {
   int warp_grid;
   int flat_grid;
 };
+
+enum { LEARN_NB_VERTICES = 0, LEARN_WARM, LEARN_SEED_WARM, LEARN_SUPPORT, LEARN_MOVED, LEARN_TARGETS };
 
 // One build of the step kernels (fast or bit-exact).
 struct KernelSet {
@@ -34,6 +37,9 @@ struct KernelSet {
   cudaError_t (*update)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st);
   cudaError_t (*unpermute)(const DevMesh& m, const float* phi, float* out, const Launch& L, cudaStream_t st);
   cudaError_t (*permute)(const DevMesh& m, const float* in, float* out, const Launch& L, cudaStream_t st);
+  // learned warm start / collection kernels (op: LEARN_*)
+  cudaError_t (*learn)(int op, const DevMesh& m, const DevState& s, const StepParams& sp, const DevLearn& lr, int arg,
+                       float fa, const Launch& L, cudaStream_t st);
 };
 const KernelSet& kernels_fast();
 const KernelSet& kernels_exact();
@@ -71,6 +77,9 @@ struct SolverStats {
   long long n_sweep = 0, n_check = 0, n_schedule = 0, n_seed = 0, n_narrowband = 0, n_update = 0;
   long long sweep_slab_bytes = 0;
   long long kernel_launches = 0;
+  // learned warm start
+  long long warm_vertices = 0, unsupported_resets = 0, support_rounds = 0, moved_vertices = 0;
+  long long learned_fallbacks = 0, pairs_collected = 0;
 };
 
 class Solver {
@@ -94,10 +103,19 @@ class Solver {
   void reset_stats();
   int status_code() const { return status_; }
   void set_profile(bool on) { cfg_.profile = on ? 1 : 0; }
+  // Learned warm start: each step's FIM starts from |network prediction| +
+  // margin (FIM frame) on the previous narrowband, followed by support checks
+  // (tolerance tol) until no warm value is left unsupported; net = null turns
+  // it off.  Collection: steps record (features, post-redistance phi / h)
+  // pairs of the previous narrowband's vertices into net's pair buffer.
+  std::string set_learned(mlp::Net* net, float margin, float tol, bool whole_patch);
+  std::string set_collect(mlp::Net* net);
 
  private:
   std::string check(cudaError_t e, const char* what);
   std::string one_step(bool* empty_nb);
+  std::string learned_step(bool* empty_nb);
+  std::string learn_buffers();
   std::string fim_loop(const StepParams& sp);
   std::string build_graph();
   void pull_stats();
@@ -121,6 +139,15 @@ class Solver {
   int status_ = 0;
   SolverStats st_;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  // learned warm start
+  mlp::Net* net_ = nullptr;      // warm start on when set
+  mlp::Net* collect_ = nullptr;  // pair collection on when set
+  float margin_ = 0.f, support_tol_ = 5e-4f;
+  bool support_patch_ = true;       // reset whole patches on an unsupported vertex
+  DevLearn lr_{};
+  int* adj_off_ = nullptr;       // vertex 1-ring CSR (product numbering)
+  int* adj_ = nullptr;
+  __nv_bfloat16* X_ = nullptr;   // features of the warm set
 };
 
 }  // namespace lsgb

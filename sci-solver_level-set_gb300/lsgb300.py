@@ -48,6 +48,9 @@ class Stats(ctypes.Structure):
         ("n_sweep", ctypes.c_longlong), ("n_check", ctypes.c_longlong), ("n_schedule", ctypes.c_longlong),
         ("n_seed", ctypes.c_longlong), ("n_narrowband", ctypes.c_longlong), ("n_update", ctypes.c_longlong),
         ("sweep_slab_bytes", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
+        ("warm_vertices", ctypes.c_longlong), ("unsupported_resets", ctypes.c_longlong),
+        ("support_rounds", ctypes.c_longlong), ("moved_vertices", ctypes.c_longlong),
+        ("learned_fallbacks", ctypes.c_longlong), ("pairs_collected", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -66,7 +69,8 @@ EXPORTS = [
     "ls_batch_get_stats", "ls_batch_reset_stats", "ls_batch_set_profile", "ls_batch_get_layout_info",
     "ls_batch_get_layout", "ls_autotune", "ls_mlp_create", "ls_mlp_destroy", "ls_mlp_last_error",
     "ls_mlp_num_params", "ls_mlp_set_params", "ls_mlp_get_params", "ls_mlp_predict", "ls_mlp_gradients",
-    "ls_mlp_train",
+    "ls_mlp_train", "ls_mlp_reserve_pairs", "ls_mlp_clear_pairs", "ls_mlp_num_pairs", "ls_mlp_train_pairs",
+    "ls_learn_collect", "ls_set_learned",
 ]
 
 class TuneTrial(ctypes.Structure):
@@ -125,6 +129,12 @@ def lib():
     L.ls_mlp_predict.argtypes = [P, V, I, V]
     L.ls_mlp_gradients.argtypes = [P, V, V, I, V, ctypes.POINTER(ctypes.c_float)]
     L.ls_mlp_train.argtypes = [P, V, V, I, I, I, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
+    L.ls_mlp_reserve_pairs.argtypes = [P, ctypes.c_longlong]
+    L.ls_mlp_clear_pairs.argtypes = [P]
+    L.ls_mlp_num_pairs.argtypes = [P, ctypes.POINTER(ctypes.c_longlong)]
+    L.ls_mlp_train_pairs.argtypes = [P, I, I, ctypes.c_float, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_float)]
+    L.ls_learn_collect.argtypes = [P, P, I, ctypes.POINTER(I)]
+    L.ls_set_learned.argtypes = [P, P, ctypes.c_double, ctypes.c_double, I]
     L.ls_batch_create.argtypes = [ctypes.POINTER(P)]
     L.ls_batch_destroy.argtypes = [P]
     L.ls_batch_last_error.argtypes = [P]
@@ -264,6 +274,16 @@ class LevelSet:
         p = Params()
         self._check(lib().ls_get_params(self._h, ctypes.byref(p)), "get_params")
         return p
+
+    def learn_collect(self, mlp, nsteps):
+        """ls_learn_collect: nsteps steps recording training pairs into mlp."""
+        done = ctypes.c_int(0)
+        self._check(lib().ls_learn_collect(self._h, mlp._m, int(nsteps), ctypes.byref(done)), "learn_collect")
+        return done.value
+
+    def set_learned(self, mlp, margin=0.0, support_tol=0.0, reset_mode=0):
+        self._check(lib().ls_set_learned(self._h, mlp._m if mlp is not None else None, float(margin),
+                                         float(support_tol), int(reset_mode)), "set_learned")
 
     def set_partition(self, npart, nparts):
         a = np.ascontiguousarray(npart, np.int32)
@@ -492,6 +512,23 @@ class MLP:
         self._check(lib().ls_mlp_gradients(self._m, _ptr(x), _ptr(t), len(x), _ptr(g), ctypes.byref(loss)),
                     "mlp gradients")
         return g, loss.value
+
+    def reserve_pairs(self, capacity):
+        self._check(lib().ls_mlp_reserve_pairs(self._m, int(capacity)), "mlp reserve_pairs")
+
+    def clear_pairs(self):
+        self._check(lib().ls_mlp_clear_pairs(self._m), "mlp clear_pairs")
+
+    def num_pairs(self):
+        n = ctypes.c_longlong(0)
+        self._check(lib().ls_mlp_num_pairs(self._m, ctypes.byref(n)), "mlp num_pairs")
+        return n.value
+
+    def train_pairs(self, epochs=1, batch=65536, lr=1e-3, seed=0):
+        loss = ctypes.c_float(0)
+        self._check(lib().ls_mlp_train_pairs(self._m, int(epochs), int(batch), float(lr), int(seed),
+                                             ctypes.byref(loss)), "mlp train_pairs")
+        return loss.value
 
     def train(self, x, t, epochs=1, batch=65536, lr=1e-3):
         x = np.ascontiguousarray(x, np.float32).reshape(-1, 128)

@@ -1,0 +1,68 @@
+"""Learned warm start on the GPU: pairs collected from this project's own
+FIM, the network trained by its tcgen05 kernels, and the warm-started step
+judged by plain FIM (support checks) -- its result stays at the plain
+step's, and the trained network's starts need fewer corrections than an
+untrained one's."""
+import numpy as np
+import pytest
+
+import lsgb300
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _band_err(a, b, w):
+    band = (np.abs(b) <= w["bandwidth"]) | (np.abs(a) <= w["bandwidth"])
+    return np.abs(a[band] - b[band]) / w["h"]
+
+
+@pytest.fixture(scope="module")
+def trained():
+    m = lsgb300.MLP(11)
+    m.reserve_pairs(1 << 20)
+    for seed in (1, 2):
+        w = synth.workload("c3", n=24, seed=seed)
+        ls = lsgb300.from_workload(w)
+        done = ls.learn_collect(m, 8)
+        assert done == 8
+        assert ls.stats()["pairs_collected"] > 0
+    n = m.num_pairs()
+    assert n > 10000
+    l0 = m.train_pairs(epochs=1, batch=4096, lr=1e-3, seed=1)
+    l1 = m.train_pairs(epochs=40, batch=4096, lr=1e-3, seed=2)
+    assert np.isfinite(l1) and l1 < l0, (l0, l1)
+    return m
+
+
+def _run(w, mlp, nsteps, margin=0.0):
+    ls = lsgb300.from_workload(w)
+    if mlp is not None:
+        ls.set_learned(mlp, margin=margin)
+    hist, done = ls.solve(nsteps)
+    return hist, done, ls.stats()
+
+
+def test_warm_start_is_judged_by_plain_fim(trained):
+    w = synth.workload("c3", n=24, seed=0)
+    ref, d0, s0 = _run(w, None, 5)
+    for mlp in (trained, lsgb300.MLP(99)):  # trained and untrained networks
+        hist, d1, s1 = _run(w, mlp, 5)
+        assert d1 == d0
+        assert s1["warm_vertices"] > 0 and s1["support_rounds"] > 0
+        for k in range(1, d0 + 1):
+            err = _band_err(hist[k], ref[k], w)
+            assert err.max() < 1e-2 and np.mean(err < 1e-3) > 0.99, (k, err.max())
+
+
+def test_trained_network_needs_fewer_corrections(trained):
+    w = synth.workload("c3", n=24, seed=0)
+    _, _, st_t = _run(w, trained, 5)
+    _, _, st_u = _run(w, lsgb300.MLP(99), 5)
+    _, _, st_p = _run(w, None, 5)
+    assert st_t["unsupported_resets"] < st_u["unsupported_resets"]
+    assert st_t["moved_vertices"] < st_u["moved_vertices"]
+    # what the warm start does to the FIM work (reported, not asserted)
+    print("plain visits %d checks %d | trained visits %d checks %d resets %d moved %d rounds %d | untrained visits %d"
+          % (st_p["patch_visits"], st_p["check_visits"], st_t["patch_visits"], st_t["check_visits"],
+             st_t["unsupported_resets"], st_t["moved_vertices"], st_t["support_rounds"], st_u["patch_visits"]))
