@@ -72,7 +72,10 @@ enum {
   /* Use the bit-exact kernel build (no FMA contraction; every float
    * operation individually rounded in the reference's order).  Slower;
    * reproduces the CPU restatement of the reference bit for bit. */
-  LS_BITEXACT = 1u << 4
+  LS_BITEXACT = 1u << 4,
+  /* ls_step_host: stage host arrays through pinned buffers even where the
+   * GPU can access pageable host memory directly (the default there). */
+  LS_HOST_STAGING = 1u << 5
 };
 
 typedef struct ls_params {

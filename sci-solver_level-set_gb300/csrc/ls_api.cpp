@@ -127,6 +127,7 @@ lsgb::SolverConfig solver_config(const ls_params& p) {
   cfg.profile = (p.flags & LS_PROFILE) ? 1 : 0;
   cfg.use_graph = (p.flags & LS_NO_GRAPH) ? 0 : 1;
   cfg.bit_exact = (p.flags & LS_BITEXACT) ? 1 : 0;
+  cfg.host_staging = (p.flags & LS_HOST_STAGING) ? 1 : 0;
   cfg.niter = p.fim_sweeps;
   cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
   cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;

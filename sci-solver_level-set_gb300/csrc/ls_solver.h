@@ -63,6 +63,7 @@ struct SolverConfig {
   double largenum = 1e9;
   double length_scale = 0.0;
   double fp64_tau = 3.814697265625e-06;  // 2^-18
+  int host_staging = 0;  // 1: host arrays go through pinned staging even where the GPU can read pageable memory
   // batches (Layout::patch_mesh set): per-mesh dt, bandwidth, curvature
   // coefficient and FIM length scale (<= 0: the mesh's mean edge)
   std::vector<double> mesh_dt, mesh_bandwidth, mesh_curv, mesh_length_scale;
@@ -136,6 +137,7 @@ class Solver {
   float* h_stage_ = nullptr;          // pinned nv floats
   float* d_tmp_ = nullptr;            // nv floats (caller-order staging)
   bool have_nb_ = false;              // previous narrowband valid (seed search restricted)
+  int pageable_ = 0;                  // the GPU can access pageable host memory directly
   int status_ = 0;
   SolverStats st_;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;

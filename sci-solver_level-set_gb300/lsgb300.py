@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liblsgb300.so")
 LS_OK, LS_BAD_INPUT, LS_PATCH_TOO_LARGE, LS_DEVICE_TIMEOUT, LS_CUDA_ERROR, LS_NOT_READY, LS_NO_MEMORY = range(7)
 UPDATE_ADVECT, UPDATE_CURVATURE, UPDATE_NONE = 0, 1, 2
 REF_COMPAT, FP64_FLAGGED, PROFILE, NO_GRAPH, BITEXACT = 1, 2, 4, 8, 16
+HOST_STAGING = 1 << 5
 
 # reference-format layout arrays (ls_get_layout selectors)
 REF_ARRAYS = {
@@ -445,10 +446,11 @@ class LevelSetBatch:
         return out
 
 
-def from_workload(w, ref_compat=False, fp64_flagged=False, profile=False, setup=True, bit_exact=False, **extra):
+def from_workload(w, ref_compat=False, fp64_flagged=False, profile=False, setup=True, bit_exact=False, flags=0,
+                  **extra):
     """LevelSet handle for a synth.workload() dictionary (mesh, partition,
     phi0, velocity and the step parameters)."""
-    flags = ((REF_COMPAT if ref_compat else 0) | (FP64_FLAGGED if fp64_flagged else 0) | (PROFILE if profile else 0)
+    flags = flags | ((REF_COMPAT if ref_compat else 0) | (FP64_FLAGGED if fp64_flagged else 0) | (PROFILE if profile else 0)
              | (BITEXACT if bit_exact else 0))
     kind = {"advect": UPDATE_ADVECT, "curvature": UPDATE_CURVATURE, "none": UPDATE_NONE}[w["update"]]
     p = default_params(num_steps=w["steps"], time_step=w["dt"], bandwidth=w["bandwidth"], update_kind=kind,

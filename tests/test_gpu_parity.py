@@ -109,13 +109,21 @@ def test_precision_form_meets_fp64_bar(update):
     assert prec.stats()["flagged_copies"] > 0
 
 
-def test_step_host_equals_device_steps():
+@pytest.mark.parametrize("staging", [False, True])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_step_host_equals_device_steps(staging, offset):
+    """ls_step_host through direct pageable access (where the GPU has it) or
+    pinned staging, with 16-byte aligned and unaligned host arrays."""
     w = synth.workload("c2", n=9)
     a = lsgb300.from_workload(w)
-    b = lsgb300.from_workload(w)
+    b = lsgb300.from_workload(w, flags=lsgb300.HOST_STAGING) if staging else lsgb300.from_workload(w)
     a.step(3)
-    phi = w["phi0"].copy()
-    out = np.empty_like(phi)
+    nv = len(w["phi0"])
+    buf_a = np.zeros(nv + 4, np.float32)
+    buf_b = np.zeros(nv + 4, np.float32)
+    phi = buf_a[offset:offset + nv]
+    out = buf_b[offset:offset + nv]
+    phi[:] = w["phi0"]
     for _ in range(3):
         b.step_host(phi, out)
         phi, out = out, phi
