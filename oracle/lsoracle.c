@@ -51,10 +51,34 @@ int lso_version(void) { return 1; }
  * src/core3d/include/redistance_kernels3d.h:124-285.  `(x) / (2.0 * p)` and
  * `/ (h + SMALLNUM)` are evaluated in double and rounded back to float, as
  * the double literals make them in the reference. */
+/* Roots of p x^2 + q x + r without cancellation (precision form): s / p
+ * (root_a) and r / s (root_b) with s = -(q + sign(q) sqrt(delta)) / 2 -- the
+ * reference's two roots (-q +- sqrt(delta)) / 2p, in an order that depends on
+ * the sign of q (every caller takes the minimum over both). */
+static float stable_s(float q, float delta) {
+  float sq = sqrtf(delta);
+  return -(q + (q >= 0.0f ? sq : -sq)) * 0.5f;
+}
+static float root_a(float p, float q, float r, float delta) { return stable_s(q, delta) / p; }
+static float root_b(float p, float q, float r, float delta) { return r / stable_s(q, delta); }
+
+/* Precision form (ill != NULL, tau > 0): a solve whose candidates cannot
+ * fall below `cutoff` (the target's current value) is skipped -- every
+ * candidate is at least min(TA, TB, TC) plus D's height over the plane ABC
+ * (Gram determinants of AC, BC, CD; taken x 0.999); otherwise a quadratic
+ * whose discriminant cancels flags the solve for an FP64 repeat, and the
+ * quadratic roots are taken in the cancellation-free form. */
 static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
                           float ACCD, float BCBC, float BCCD, float CDCD,
-                          double eps_h, float LN, float tau, int* ill, int fdiv) {
+                          double eps_h, float LN, float tau, int* ill, int fdiv, float cutoff) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
+  if (ill) {
+    float det2 = ACAC * BCBC - ACBC * ACBC;
+    float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
+                 ACCD * (ACBC * BCCD - BCBC * ACCD);
+    float lb = fminf(fminf(TA, TB), TC) + 0.999f * sqrtf(fmaxf(det3 / det2, 0.0f));
+    if (lb >= cutoff) return LN;
+  }
   float p, q, r, lambda1, lambda2, lambda3;
   float FaceTAC = LN, FaceTAB = LN, FaceTBC = LN;
   float delta, TE, TD = LN;
@@ -68,14 +92,14 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
     lambda1 = 0.0f;
-    lambda2 = (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
+    lambda2 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda3 = 1 - lambda1 - lambda2;
     if (lambda2 >= 0 && lambda2 <= 1) {
       TE = TB * lambda2 + TC * lambda3;
       FaceTBC = fminf(FaceTBC, TE + sqrtf((lambda2 * BCBC + BCCD) * lambda2 + (lambda2 * BCCD + CDCD)));
     }
     lambda1 = 0.0f;
-    lambda2 = (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
+    lambda2 = ill ? root_b(p, q, r, delta) : (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
     lambda3 = 1 - lambda1 - lambda2;
     if (lambda2 >= 0 && lambda2 <= 1) {
       TE = TB * lambda2 + TC * lambda3;
@@ -95,7 +119,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   delta = q * q - 4 * p * r;
   if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
-    lambda1 = (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
+    lambda1 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = 1 - lambda1;
     if (lambda1 >= 0 && lambda1 <= 1) {
       TE = TA * lambda1 + TB * lambda2;
@@ -103,7 +127,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
                                           (lambda1 * ACBC + lambda2 * BCBC + BCCD) * lambda2 +
                                           (lambda1 * ACCD + lambda2 * BCCD + CDCD)));
     }
-    lambda1 = (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
+    lambda1 = ill ? root_b(p, q, r, delta) : (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = 1 - lambda1;
     if (lambda1 >= 0 && lambda1 <= 1) {
       TE = TA * lambda1 + TB * lambda2;
@@ -121,14 +145,14 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   delta = q * q - 4 * p * r;
   if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
-    lambda1 = (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
+    lambda1 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = 0.0f;
     lambda3 = 1 - lambda1 - lambda2;
     if (lambda1 >= 0 && lambda1 <= 1) {
       TE = TA * lambda1 + TC * lambda3;
       FaceTAC = fminf(FaceTAC, TE + sqrtf((lambda1 * ACAC + ACCD) * lambda1 + (lambda1 * ACCD + CDCD)));
     }
-    lambda1 = (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
+    lambda1 = ill ? root_b(p, q, r, delta) : (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = 0.0f;
     lambda3 = 1 - lambda1 - lambda2;
     if (lambda1 >= 0 && lambda1 <= 1) {
@@ -151,7 +175,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   delta = q * q - 4 * p * r;
   if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
-    lambda1 = (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
+    lambda1 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = fdiv ? (s * lambda1 + t) / (h + (float)eps_h)
                    : (float)((double)(s * lambda1 + t) / ((double)h + eps_h));
     lambda3 = 1 - lambda1 - lambda2;
@@ -161,7 +185,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
                                 (lambda1 * ACBC + lambda2 * BCBC + BCCD) * lambda2 +
                                 (lambda1 * ACCD + lambda2 * BCCD + CDCD)));
     }
-    lambda1 = (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
+    lambda1 = ill ? root_b(p, q, r, delta) : (float)((double)(-q - sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = fdiv ? (s * lambda1 + t) / (h + (float)eps_h)
                    : (float)((double)(s * lambda1 + t) / ((double)h + eps_h));
     lambda3 = 1 - lambda1 - lambda2;
@@ -179,7 +203,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
 float lso_tet_solve_f32(float TA, float TB, float TC, float ACAC, float ACBC,
                         float ACCD, float BCBC, float BCCD, float CDCD,
                         double eps_h, float LN) {
-  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL, 0);
+  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL, 0, INFINITY);
 }
 
 /* The same solver with every quantity in double (the FP64 oracle). */
@@ -271,9 +295,9 @@ double lso_tet_solve_f64(double TA, double TB, double TC, double ACAC,
 
 static float tet_f32_flagged(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
                              float BCBC, float BCCD, float CDCD, double eps_h, float LN, float tau,
-                             int* flagged, int fdiv) {
+                             int* flagged, int fdiv, float cutoff) {
   int ill = 0;
-  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill, fdiv);
+  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill, fdiv, cutoff);
   if (flagged) *flagged = ill;
   if (!ill) return r;
   return (float)lso_tet_solve_f64(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
@@ -283,7 +307,7 @@ float lso_tet_solve_f32_flagged(float TA, float TB, float TC, float ACAC, float 
                                 float ACCD, float BCBC, float BCCD, float CDCD,
                                 double eps_h, float LN, float tau, int* flagged) {
   int ill = 0;
-  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill, 0);
+  float r = tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, tau, &ill, 0, INFINITY);
   if (flagged) *flagged = ill;
   if (!ill) return r;
   return (float)lso_tet_solve_f64(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
@@ -314,10 +338,11 @@ static void copy_coords_f32(const lso_layout* lo, const struct ctx_f32* cx, int 
  * (s l1 + t) / (h + SMALLNUM) is evaluated in float (the GPU does the same);
  * with them, in double as the reference's double SMALLNUM makes it. */
 static float tet_f32(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD, float BCBC,
-                     float BCCD, float CDCD, double eps_h, float LN, double tau, int fdiv) {
+                     float BCCD, float CDCD, double eps_h, float LN, double tau, int fdiv, float cutoff) {
   if (tau > 0)
-    return tet_f32_flagged(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, (float)tau, NULL, fdiv);
-  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL, fdiv);
+    return tet_f32_flagged(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, (float)tau, NULL, fdiv,
+                           cutoff);
+  return tet_f32_impl(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN, 0.f, NULL, fdiv, INFINITY);
 }
 #include "lso_real.inc"
 #undef REAL
@@ -347,9 +372,11 @@ static void copy_coords_f64(const lso_layout* lo, const struct ctx_f64* cx, int 
   for (int i = 0; i < nc; ++i) L[i] = cx->lc[(size_t)c * nc + i];
 }
 static double tet_f64(double TA, double TB, double TC, double ACAC, double ACBC, double ACCD,
-                      double BCBC, double BCCD, double CDCD, double eps_h, double LN, double tau, int fdiv) {
+                      double BCBC, double BCCD, double CDCD, double eps_h, double LN, double tau, int fdiv,
+                      double cutoff) {
   (void)tau;
   (void)fdiv;
+  (void)cutoff;
   return lso_tet_solve_f64(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, LN);
 }
 #include "lso_real.inc"

@@ -126,10 +126,38 @@ __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a,
 // `tau` > 0 turns on the conditioning check of the precision form: `ill` is
 // set when a discriminant q^2 - 4pr cancels, |q^2 - 4pr| <= tau (q^2 + |4pr|),
 // i.e. when FP32 has lost about log2(1/tau) bits of it.
+// Roots of p x^2 + q x + r given sq = sqrt(q^2 - 4pr).  The reference's
+// form (-q +- sq) / 2p, or, for the precision form, the cancellation-free
+// pair s / p, r / s with s = -(q + sign(q) sq) / 2 (the same two roots; also
+// right when p = 0).
+template <typename R, bool STABLE>
+__device__ __forceinline__ void roots(R p, R q, R r, R sq, R& ra, R& rb) {
+  if (STABLE) {
+    const R sh = -(q + (q >= R(0) ? sq : -sq)) * R(0.5);
+    ra = sh / p;
+    rb = r / sh;
+  } else {
+    ra = (-q + sq) / (R(2) * p);
+    rb = (-q - sq) / (R(2) * p);
+  }
+}
+
 template <typename R, bool XDIV, bool CHK = true>
 __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD, R BCBC, R BCCD,
-                                       R CDCD, R eps_h, double eps_h64, R LN, R tau, bool& ill) {
+                                       R CDCD, R eps_h, double eps_h64, R LN, R tau, bool& ill,
+                                       R cutoff = R(0)) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
+  if (CHK) {
+    // precision form: a solve whose candidates cannot fall below `cutoff`
+    // (the target's current value) is skipped -- every candidate is at
+    // least min(TA, TB, TC) plus D's height over the plane ABC (Gram
+    // determinants of AC, BC, CD; taken x 0.999)
+    const R det2 = ACAC * BCBC - ACBC * ACBC;
+    const R det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
+                   ACCD * (ACBC * BCCD - BCBC * ACCD);
+    const R lb = rmin(rmin(TA, TB), TC) + R(0.999) * sqrt(fmax(det3 / det2, R(0)));
+    if (lb >= cutoff) return LN;
+  }
   const R two = R(2), four = R(4), one = R(1), zero = R(0);
   R p, q, r, lambda1, lambda2, lambda3, delta, TE;
   R FaceTAC = LN, FaceTAB = LN, FaceTBC = LN, TD = LN;
@@ -143,14 +171,16 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
+    R ra, rb;
+    roots<R, CHK>(p, q, r, sq, ra, rb);
     lambda1 = zero;
-    lambda2 = (-q + sq) / (two * p);
+    lambda2 = ra;
     lambda3 = one - lambda1 - lambda2;
     if (lambda2 >= zero && lambda2 <= one) {
       TE = TB * lambda2 + TC * lambda3;
       FaceTBC = rmin(FaceTBC, TE + sqrt((lambda2 * BCBC + BCCD) * lambda2 + (lambda2 * BCCD + CDCD)));
     }
-    lambda2 = (-q - sq) / (two * p);
+    lambda2 = rb;
     lambda3 = one - lambda1 - lambda2;
     if (lambda2 >= zero && lambda2 <= one) {
       TE = TB * lambda2 + TC * lambda3;
@@ -171,9 +201,11 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
+    R ra, rb;
+    roots<R, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      lambda1 = (-q + (sgn ? -sq : sq)) / (two * p);
+      lambda1 = sgn ? rb : ra;
       lambda2 = one - lambda1;
       if (lambda1 >= zero && lambda1 <= one) {
         TE = TA * lambda1 + TB * lambda2;
@@ -193,9 +225,11 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
+    R ra, rb;
+    roots<R, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      lambda1 = (-q + (sgn ? -sq : sq)) / (two * p);
+      lambda1 = sgn ? rb : ra;
       lambda3 = one - lambda1 - zero;
       if (lambda1 >= zero && lambda1 <= one) {
         TE = TA * lambda1 + TC * lambda3;
@@ -219,9 +253,11 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
+    R ra, rb;
+    roots<R, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      lambda1 = (-q + (sgn ? -sq : sq)) / (two * p);
+      lambda1 = sgn ? rb : ra;
       if (XDIV)
         lambda2 = (R)((double)(s * lambda1 + t) / ((double)h + eps_h64));
       else

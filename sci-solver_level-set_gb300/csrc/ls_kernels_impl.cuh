@@ -103,10 +103,10 @@ __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], fl
     const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
     const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
     bool ill[4] = {false, false, false, false};
-    float r3 = tet_solve<float, XDIV, PREC>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3]);
-    float r0 = tet_solve<float, XDIV, PREC>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0]);
-    float r1 = tet_solve<float, XDIV, PREC>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1]);
-    float r2 = tet_solve<float, XDIV, PREC>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2]);
+    float r3 = tet_solve<float, XDIV, PREC>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3], TD);
+    float r0 = tet_solve<float, XDIV, PREC>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0], TA);
+    float r1 = tet_solve<float, XDIV, PREC>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1], TB);
+    float r2 = tet_solve<float, XDIV, PREC>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2], TC);
     if (PREC && (ill[0] | ill[1] | ill[2] | ill[3])) {
       const double L64 = LN;
       bool d = false;
@@ -128,6 +128,47 @@ __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], fl
     out[3] = LN;
   }
 }
+
+// Precision form, deferred: the FP32 solves of one tet copy with their
+// ill-conditioning flags (the FP64 repeats run later, compacted over the CTA).
+template <bool XDIV>
+__device__ __forceinline__ void solve_copy_flags(const float* Mt, const float T[4], float r[4], bool ill[4],
+                                                 float eps_h, double eps_h64, float LN, float tau) {
+  const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4];
+  const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
+  const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
+  ill[0] = ill[1] = ill[2] = ill[3] = false;
+  r[3] = tet_solve<float, XDIV, true>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3], TD);
+  r[0] = tet_solve<float, XDIV, true>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0], TA);
+  r[1] = tet_solve<float, XDIV, true>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1], TB);
+  r[2] = tet_solve<float, XDIV, true>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2], TC);
+}
+
+// The FP64 repeat of solve k of a tet copy (same argument order as above).
+__device__ __noinline__ float solve_k_fp64(const float* Mt, const float T[4], int k, double eps_h64, float LN) {
+  const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4];
+  const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
+  const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
+  const double L64 = LN;
+  bool d = false;
+  double r;
+  switch (k) {
+    case 3: r = tet_solve<double, false, false>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h64, eps_h64, L64, 0.0, d); break;
+    case 0: r = tet_solve<double, false, false>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h64, eps_h64, L64, 0.0, d); break;
+    case 1: r = tet_solve<double, false, false>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h64, eps_h64, L64, 0.0, d); break;
+    default: r = tet_solve<double, false, false>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h64, eps_h64, L64, 0.0, d); break;
+  }
+  return (float)r;
+}
+
+// One deferred FP64 solve: the copy (CTA-local index << 2 | solve) and its
+// four values at the start of the sweep; res = min(T_k, FP64 result).
+struct DeferredSolve {
+  int code;
+  float t[4];
+  float res;
+};
+constexpr int kDeferCap = 1024;
 
 template <int D1>
 __device__ __forceinline__ void copy_metric(const DevMesh& m, long long c, float* Mt) {
@@ -179,6 +220,9 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
   float* sT = smem;                       // owned + ghost values
   float* sOld = smem + sp.lvp + sp.lgp;   // owned values at the start of the last sweep
   __shared__ unsigned s_min;
+  __shared__ int s_qn;  // deferred FP64 solves queued in this sweep (precision form)
+  DeferredSolve* sQ = reinterpret_cast<DeferredSolve*>(smem + 2 * sp.lvp + sp.lgp);
+  if (PREC && threadIdx.x == 0) s_qn = 0;
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -223,9 +267,35 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
         for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
         __syncthreads();
       }
+      int qpos[4] = {-1, -1, -1, -1};
       if (act) {
         float nw[4];
-        solve_copy<D1, XDIV, PREC>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau, nflag);
+        if constexpr (PREC && D1 == 4) {
+          // FP32 solves; flagged ones go to the CTA's queue for one
+          // compacted FP64 pass after the sweep (inline if the queue is full)
+          float rr[4];
+          bool ill[4];
+          solve_copy_flags<XDIV>(Mt, T, rr, ill, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (ill[k]) {
+              const int pos = atomicAdd(&s_qn, 1);
+              if (pos < kDeferCap) {
+                DeferredSolve& e = sQ[pos];
+                e.code = (tid << 2) | k;
+                e.t[0] = T[0]; e.t[1] = T[1]; e.t[2] = T[2]; e.t[3] = T[3];
+                qpos[k] = pos;
+                rr[k] = sp.largenum;
+              } else {
+                rr[k] = solve_k_fp64(Mt, T, k, sp.eps_h64, sp.largenum);
+                nflag++;
+              }
+            }
+            nw[k] = fminf(T[k], rr[k]);
+          }
+        } else {
+          solve_copy<D1, XDIV, PREC>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau, nflag);
+        }
 #pragma unroll
         for (int k = 0; k < D1; ++k) {
           if (idx[k] < nvp) atomicMin(reinterpret_cast<int*>(&sT[idx[k]]), __float_as_int(nw[k]));
@@ -233,6 +303,28 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
         }
       }
       __syncthreads();
+      if constexpr (PREC && D1 == 4) {
+        const int nq = min(s_qn, kDeferCap);
+        for (int i = tid; i < nq; i += blockDim.x) {
+          DeferredSolve& e = sQ[i];
+          const int cl = e.code >> 2, k = e.code & 3;
+          float Mq[11];
+          copy_metric<D1>(m, (long long)es + cl, Mq);
+          const float res = fminf(e.t[k], solve_k_fp64(Mq, e.t, k, sp.eps_h64, sp.largenum));
+          const ushort4 cv = m.conn[es + cl];
+          const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
+          if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(res));
+          else e.res = res;
+          nflag++;
+        }
+        __syncthreads();
+        if (act) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (qpos[k] >= 0 && idx[k] >= nvp) T[k] = sQ[qpos[k]].res;
+        }
+        if (tid == 0) s_qn = 0;
+      }
       if (act) {
 #pragma unroll
         for (int k = 0; k < D1; ++k)
@@ -858,11 +950,15 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
   const bool xd = sp.xdiv != 0;
   const bool pr = sp.tau > 0.f;
   const int c = check ? 1 : 0;
-#define LS_FIM(D, T, X, B, P) k_fim<D, T, X, B, P><<<L.fim_grid, L.fim_block, L.fim_smem, st>>>(m, s, sp, cur, c)
+  // precision-form kernels: one 384-class register budget (2 CTAs/SM) and
+  // the deferred-solve queue in shared memory
+  const int psmem = L.fim_smem + (int)sizeof(DeferredSolve) * kDeferCap;
+#define LS_FIM(D, T, X, B, P) \
+  k_fim<D, T, X, B, P><<<L.fim_grid, L.fim_block, P ? psmem : L.fim_smem, st>>>(m, s, sp, cur, c)
 #define LS_FIM3(T, B) \
   do { \
-    if (xd) { if (pr) LS_FIM(4, T, true, B, true); else LS_FIM(4, T, true, B, false); } \
-    else { if (pr) LS_FIM(4, T, false, B, true); else LS_FIM(4, T, false, B, false); } \
+    if (xd) { if (pr) LS_FIM(4, T, true, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, true, B, false); } \
+    else { if (pr) LS_FIM(4, T, false, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, false, B, false); } \
   } while (0)
   if (m.dim == 3) {
     if (L.fim_block <= 384) {
