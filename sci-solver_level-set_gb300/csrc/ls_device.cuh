@@ -142,12 +142,12 @@ __device__ __forceinline__ void roots(R p, R q, R r, R sq, R& ra, R& rb) {
   }
 }
 
-template <typename R, bool XDIV, bool CHK = true>
+template <typename R, bool XDIV, bool CHK = true, bool LB = false>
 __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD, R BCBC, R BCCD,
                                        R CDCD, R eps_h, double eps_h64, R LN, R tau, bool& ill,
                                        R cutoff = R(0)) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
-  if (CHK) {
+  if (CHK || LB) {
     // precision form: a solve whose candidates cannot fall below `cutoff`
     // (the target's current value) is skipped -- every candidate is at
     // least min(TA, TB, TC) plus D's height over the plane ABC (Gram

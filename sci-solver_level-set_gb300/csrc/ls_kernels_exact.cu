@@ -7,6 +7,7 @@
 #include "ls_device.cuh"
 #include "ls_solver.h"
 
+#define LS_KERNELS_EXACT 1
 namespace lsgb {
 namespace exact {
 #include "ls_kernels_impl.cuh"

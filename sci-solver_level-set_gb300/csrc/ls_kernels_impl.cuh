@@ -95,6 +95,17 @@ __global__ void k_seed(DevMesh m, DevState s, int use_all, float scale, int warm
 // Solves of one element copy (Jacobi: all from the values at sweep start).
 // With the precision form (tau > 0) a solve whose discriminant cancelled is
 // repeated in FP64; `nflag` counts those repeats.
+// Fast build: a tet solve whose candidates provably cannot fall below the
+// target's current value (min(TA, TB, TC) + 0.999 x D's height over the
+// base plane >= T_D) is skipped -- in exact arithmetic it cannot change
+// min(T_D, r).  The bit-exact build keeps every solve (the reference's
+// arithmetic, including FP32 candidates that fall below that bound).
+#ifdef LS_KERNELS_EXACT
+constexpr bool kLbSkip = false;
+#else
+constexpr bool kLbSkip = true;
+#endif
+
 template <int D1, bool XDIV, bool PREC>
 __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], float out[4], float eps_h,
                                            double eps_h64, float LN, float tau, int& nflag) {
@@ -103,10 +114,10 @@ __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], fl
     const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
     const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
     bool ill[4] = {false, false, false, false};
-    float r3 = tet_solve<float, XDIV, PREC>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3], TD);
-    float r0 = tet_solve<float, XDIV, PREC>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0], TA);
-    float r1 = tet_solve<float, XDIV, PREC>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1], TB);
-    float r2 = tet_solve<float, XDIV, PREC>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2], TC);
+    float r3 = tet_solve<float, XDIV, PREC, kLbSkip>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3], TD);
+    float r0 = tet_solve<float, XDIV, PREC, kLbSkip>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0], TA);
+    float r1 = tet_solve<float, XDIV, PREC, kLbSkip>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1], TB);
+    float r2 = tet_solve<float, XDIV, PREC, kLbSkip>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2], TC);
     if (PREC && (ill[0] | ill[1] | ill[2] | ill[3])) {
       const double L64 = LN;
       bool d = false;
