@@ -381,6 +381,177 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
   }
 }
 
+// Fast-build FIM patch visit for tetrahedra with compacted solves.  Same
+// visit semantics as k_fim (Jacobi within an element, private ghost values,
+// per-vertex minimum, convergence on the last sweep), reorganised so that
+// the warps only run solves that can change something: at the start of each
+// sweep every element copy tests its four solves with the lower bound of
+// solve_copy (min of the three other values + 0.999 x height >= own value
+// -> cannot lower it) and appends the others to a CTA list; all threads
+// then run the listed solves densely, one solve per thread at a time.
+// Shared memory per CTA (stride MAXT): metric [11], heights [4], copy
+// values at the sweep start [4], ghost results [4], connectivity, list.
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState s, StepParams sp, int cur,
+                                                            int check) {
+  const bool CHECK = check != 0;
+  extern __shared__ float smem[];
+  float* sT = smem;                       // owned + ghost values
+  float* sOld = smem + sp.lvp + sp.lgp;   // owned values at the start of the last sweep
+  float* sM = smem + ((2 * sp.lvp + sp.lgp + 3) & ~3);  // [11][MAXT] metric (16-byte aligned)
+  float* sH = sM + 11 * MAXT;             // [4][MAXT] heights of A, B, C, D
+  float* sTc = sH + 4 * MAXT;             // [4][MAXT] copy values at the sweep start
+  float* sR = sTc + 4 * MAXT;             // [4][MAXT] results for ghost targets
+  ushort4* sC = reinterpret_cast<ushort4*>(sR + 4 * MAXT);  // [MAXT] connectivity
+  int* sItem = reinterpret_cast<int*>(sC + MAXT);           // [4 * MAXT] listed solves (copy << 2 | k)
+  __shared__ unsigned s_min;
+  __shared__ int s_n;
+  const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
+  const int count = CHECK ? s.counts[2] : s.counts[cur];
+  const int nxt = cur ^ 1;
+  int* nlist = nxt ? s.list1 : s.list0;
+  if (!CHECK && blockIdx.x == 0 && threadIdx.x == 0) {
+    s.counts[nxt] = 0;
+    s.counts[2] = 0;
+    if (count > 0) {
+      s.counts[4] += 1;
+      atomicAdd(&s.stats[5], 1ull);
+    }
+    atomicAdd(&s.stats[0], (unsigned long long)count);
+  }
+  if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
+  const int niter = CHECK ? 1 : sp.niter;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_n = 0;
+  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+    const int p = list[li];
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
+    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+    for (int i = tid; i < nvp + ngp; i += blockDim.x)
+      sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
+    if (tid == 0) s_min = 0x7f800000u;
+    __syncthreads();
+    const bool act = tid < nep;
+    int idx[4] = {0, 0, 0, 0};
+    float T[4] = {0.f, 0.f, 0.f, 0.f};
+    float hgt[4] = {0.f, 0.f, 0.f, 0.f};
+    if (act) {
+      const ushort4 cv = m.conn[es + tid];
+      sC[tid] = cv;
+      idx[0] = cv.x; idx[1] = cv.y; idx[2] = cv.z; idx[3] = cv.w;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) T[k] = sT[idx[k]];
+      float Mt[11];
+      copy_metric<4>(m, (long long)es + tid, Mt);
+#pragma unroll
+      for (int j = 0; j < 11; ++j) sM[j * MAXT + tid] = Mt[j];
+      const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
+      const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
+      const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
+                         ACCD * (ACBC * BCCD - BCBC * ACCD);
+      hgt[0] = sqrtf(fmaxf(det3 / (BCBC * CDCD - BCCD * BCCD), 0.f));  // A over BCD
+      hgt[1] = sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f));  // B over ACD
+      hgt[2] = sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f));  // C over ABD
+      hgt[3] = sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f));  // D over ABC
+    }
+#pragma unroll 1
+    for (int it = 0; it < niter; ++it) {
+      if (it == niter - 1) {
+        for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
+        __syncthreads();
+      }
+      // list the solves that can lower their target
+      unsigned need = 0;
+      if (act) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) sTc[k * MAXT + tid] = T[k];
+        const float LN = sp.largenum;
+        const float m012 = fminf(fminf(T[0], T[1]), T[2]), m013 = fminf(fminf(T[0], T[1]), T[3]);
+        const float m023 = fminf(fminf(T[0], T[2]), T[3]), m123 = fminf(fminf(T[1], T[2]), T[3]);
+        // apex k: the other three values all LARGENUM -> LARGENUM (as tet_solve)
+        if (m123 < LN && m123 + 0.999f * hgt[0] < T[0]) need |= 1u;
+        if (m023 < LN && m023 + 0.999f * hgt[1] < T[1]) need |= 2u;
+        if (m013 < LN && m013 + 0.999f * hgt[2] < T[2]) need |= 4u;
+        if (m012 < LN && m012 + 0.999f * hgt[3] < T[3]) need |= 8u;
+        const int n = __popc(need);
+        if (n) {
+          int pos = atomicAdd(&s_n, n);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (need & (1u << k)) sItem[pos++] = (tid << 2) | k;
+        }
+      }
+      __syncthreads();
+      const int nitems = s_n;
+      for (int i = tid; i < nitems; i += blockDim.x) {
+        const int code = sItem[i];
+        const int cc = code >> 2, k = code & 3;
+        const float TA = sTc[cc], TB = sTc[MAXT + cc], TC = sTc[2 * MAXT + cc], TD = sTc[3 * MAXT + cc];
+        const float ACAC = sM[cc], ACBC = sM[MAXT + cc], ACCD = sM[2 * MAXT + cc], BCBC = sM[3 * MAXT + cc];
+        const float BCCD = sM[4 * MAXT + cc], CDCD = sM[5 * MAXT + cc], ADAD = sM[6 * MAXT + cc];
+        const float ADBD = sM[7 * MAXT + cc], ADCD = sM[8 * MAXT + cc], BDBD = sM[9 * MAXT + cc];
+        const float CDBD = sM[10 * MAXT + cc];
+        // the permuted arguments of solve k (solve_copy's four calls)
+        float a0, a1, a2, g0, g1, g2, g3, g4, g5, own;
+        if (k == 3) { a0 = TA; a1 = TB; a2 = TC; g0 = ACAC; g1 = ACBC; g2 = ACCD; g3 = BCBC; g4 = BCCD; g5 = CDCD; own = TD; }
+        else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
+        else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
+        else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
+        bool d = false;
+        const float r = tet_solve<float, false, false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.eps_h64,
+                                                       sp.largenum, 0.f, d);
+        const float nw = fminf(own, r);
+        const ushort4 cv = sC[cc];
+        const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
+        if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(nw));
+        else sR[k * MAXT + cc] = nw;
+      }
+      __syncthreads();
+      if (tid == 0) s_n = 0;
+      if (act) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (idx[k] < nvp) T[k] = sT[idx[k]];
+          else if (need & (1u << k)) T[k] = sR[k * MAXT + tid];
+        }
+      }
+      __syncthreads();
+    }
+    int con = 1;
+    for (int i = tid; i < nvp; i += blockDim.x) {
+      const int v = vs + i;
+      const float nt = sT[i];
+      float outv;
+      if (!s.seed[v]) {
+        if (!CHECK) s.DT_out[v] = nt;
+        con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
+        outv = nt;
+      } else {
+        outv = s.DT[v];
+      }
+      if (!CHECK) atomicMin(&s_min, __float_as_uint(outv));
+    }
+    con = __syncthreads_and(con);
+    if (tid == 0) {
+      if (!CHECK) {
+        atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
+        s.bcon[p] = con;
+        s.bmin[p] = __uint_as_float(s_min);
+        s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
+      } else {
+        if (!con) {
+          const int pos = atomicAdd(&s.counts[nxt], 1);
+          nlist[pos] = p;
+        } else {
+          s.blabel[p] = LS_FAR;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Schedule of one FIM iteration: one warp per patch of the current list.
 __global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
   const int count = s.counts[cur];
@@ -956,6 +1127,12 @@ cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float 
 // Block size classes: patches of up to 384 element copies run 2, 3 or 4
 // CTAs per SM (registers capped at 85 / 56 / 42; StepParams::ctas), larger
 // ones one CTA of 512 or 1024 threads.
+// dynamic shared memory of k_fim_compact<MAXT>: slab + owned snapshot
+// (rounded up to 16 bytes), then 23 floats, one ushort4 and 4 ints per thread
+inline int compact_smem(const StepParams& sp, int maxt) {
+  return (int)sizeof(float) * (((2 * sp.lvp + sp.lgp + 3) & ~3) + 23 * maxt) + 8 * maxt + 16 * maxt;
+}
+
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
                          const Launch& L, cudaStream_t st) {
   const bool xd = sp.xdiv != 0;
@@ -971,7 +1148,19 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
     if (xd) { if (pr) LS_FIM(4, T, true, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, true, B, false); } \
     else { if (pr) LS_FIM(4, T, false, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, false, B, false); } \
   } while (0)
-  if (m.dim == 3) {
+  if (kLbSkip && m.dim == 3 && !pr) {
+    // fast build, tetrahedra: compacted solves
+    const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
+    if (L.fim_block <= 384) {
+      if (sp.ctas == 2) k_fim_compact<384, 2><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      else if (sp.ctas == 4) k_fim_compact<384, 4><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      else k_fim_compact<384, 3><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+    } else if (L.fim_block <= 512) {
+      k_fim_compact<512, 1><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+    } else {
+      k_fim_compact<1024, 1><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+    }
+  } else if (m.dim == 3) {
     if (L.fim_block <= 384) {
       if (sp.ctas == 2) LS_FIM3(384, 2);
       else if (sp.ctas == 4) LS_FIM3(384, 4);
@@ -1035,7 +1224,28 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   if (L.fim_block < 64) L.fim_block = 64;
   L.fim_smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
   int occ = 0;
-  if (m.dim == 3) {
+  if (kLbSkip && m.dim == 3) {
+    // compacted kernel (fast build): opt in to its shared memory, size the
+    // grid by its occupancy
+    const int maxt = L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024;
+    const int cs = compact_smem(sp, maxt);
+    if (L.fim_block <= 384 && sp.ctas == 2) {
+      e = cudaFuncSetAttribute(k_fim_compact<384, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 2>, L.fim_block, cs);
+    } else if (L.fim_block <= 384 && sp.ctas == 4) {
+      e = cudaFuncSetAttribute(k_fim_compact<384, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 4>, L.fim_block, cs);
+    } else if (L.fim_block <= 384) {
+      e = cudaFuncSetAttribute(k_fim_compact<384, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 3>, L.fim_block, cs);
+    } else if (L.fim_block <= 512) {
+      e = cudaFuncSetAttribute(k_fim_compact<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<512, 1>, L.fim_block, cs);
+    } else {
+      e = cudaFuncSetAttribute(k_fim_compact<1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<1024, 1>, L.fim_block, cs);
+    }
+  } else if (m.dim == 3) {
     if (L.fim_block <= 384 && sp.ctas == 2)
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 2, false>, L.fim_block, L.fim_smem);
     else if (L.fim_block <= 384 && sp.ctas == 4)
