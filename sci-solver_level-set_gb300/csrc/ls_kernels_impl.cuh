@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   ushort4* sC = reinterpret_cast<ushort4*>(sR + 4 * MAXT);  // [MAXT] connectivity
   int* sItem = reinterpret_cast<int*>(sC + MAXT);           // [4 * MAXT] listed solves (copy << 2 | k)
   __shared__ unsigned s_min;
-  __shared__ int s_n;
+  __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  if (tid == 0) s_n = 0;
+  if (tid == 0) s_n[0] = s_n[1] = 0;
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
     const int p = list[li];
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
@@ -476,14 +476,17 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         if (m012 < LN && m012 + 0.999f * hgt[3] < T[3]) need |= 8u;
         const int n = __popc(need);
         if (n) {
-          int pos = atomicAdd(&s_n, n);
+          int pos = atomicAdd(&s_n[it & 1], n);
 #pragma unroll
           for (int k = 0; k < 4; ++k)
             if (need & (1u << k)) sItem[pos++] = (tid << 2) | k;
         }
       }
       __syncthreads();
-      const int nitems = s_n;
+      const int nitems = s_n[it & 1];
+      // the other parity's counter is idle until the next sweep's listing,
+      // which starts after the barrier below
+      if (tid == 0) s_n[(it & 1) ^ 1] = 0;
       for (int i = tid; i < nitems; i += blockDim.x) {
         const int code = sItem[i];
         const int cc = code >> 2, k = code & 3;
@@ -508,7 +511,6 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         else sR[k * MAXT + cc] = nw;
       }
       __syncthreads();
-      if (tid == 0) s_n = 0;
       if (act) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -516,8 +518,11 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
           else if (need & (1u << k)) T[k] = sR[k * MAXT + tid];
         }
       }
-      __syncthreads();
+      // no barrier here: the next sweep's solves change sT only after the
+      // barrier that follows its listing (Jacobi order is kept)
     }
+    __syncthreads();
+    if (tid == 0) s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
     int con = 1;
     for (int i = tid; i < nvp; i += blockDim.x) {
       const int v = vs + i;
