@@ -35,6 +35,21 @@ METRIC = "narrowband vertex-updates/s (curvature flow, 128^3 jittered cube, 3 sp
 UNIT = "vertex-updates/s"
 
 
+def job_totals(ms, updates, dist=None):
+    """Whole-job timing over independent replicas: the slowest rank's time
+    and the sum of all ranks' narrowband vertex-updates."""
+    if dist is None:
+        return ms, float(updates)
+    import torch
+
+    t = torch.tensor([ms, float(updates)], dtype=torch.float64)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    tsum = t.clone()
+    dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(tsum[1])
+
+
 def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -389,15 +404,7 @@ def main():
     clocks.stop()
     st = ls.stats()
     updates = st["nb_vertex_updates"]
-    if dist is not None:
-        t = torch.tensor([ms, float(updates)], dtype=torch.float64)
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        tsum = t.clone()
-        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
-        ms_job, updates_job = float(tmax[0]), float(tsum[1])
-    else:
-        ms_job, updates_job = ms, float(updates)
+    ms_job, updates_job = job_totals(ms, updates, dist)
     value = updates_job / (ms_job / 1000.0)
     # our kernels launched inside the timed region (graph kernels included)
     gpu_launches = int(st["kernel_launches"])
