@@ -455,6 +455,10 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       hgt[2] = sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f));  // C over ABD
       hgt[3] = sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f));  // D over ABC
     }
+    // vertices of this copy whose value changed in the previous sweep (all
+    // on the first): a solve whose three inputs are unchanged returns what
+    // it returned before, which cannot lower its target again
+    unsigned chg = 0xFu;
 #pragma unroll 1
     for (int it = 0; it < niter; ++it) {
       if (it == niter - 1) {
@@ -470,10 +474,10 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         const float m012 = fminf(fminf(T[0], T[1]), T[2]), m013 = fminf(fminf(T[0], T[1]), T[3]);
         const float m023 = fminf(fminf(T[0], T[2]), T[3]), m123 = fminf(fminf(T[1], T[2]), T[3]);
         // apex k: the other three values all LARGENUM -> LARGENUM (as tet_solve)
-        if (m123 < LN && m123 + 0.999f * hgt[0] < T[0]) need |= 1u;
-        if (m023 < LN && m023 + 0.999f * hgt[1] < T[1]) need |= 2u;
-        if (m013 < LN && m013 + 0.999f * hgt[2] < T[2]) need |= 4u;
-        if (m012 < LN && m012 + 0.999f * hgt[3] < T[3]) need |= 8u;
+        if ((chg & 0xEu) && m123 < LN && m123 + 0.999f * hgt[0] < T[0]) need |= 1u;
+        if ((chg & 0xDu) && m023 < LN && m023 + 0.999f * hgt[1] < T[1]) need |= 2u;
+        if ((chg & 0xBu) && m013 < LN && m013 + 0.999f * hgt[2] < T[2]) need |= 4u;
+        if ((chg & 0x7u) && m012 < LN && m012 + 0.999f * hgt[3] < T[3]) need |= 8u;
         const int n = __popc(need);
         if (n) {
           int pos = atomicAdd(&s_n[it & 1], n);
@@ -512,10 +516,13 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       }
       __syncthreads();
       if (act) {
+        chg = 0u;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
+          const float old = T[k];
           if (idx[k] < nvp) T[k] = sT[idx[k]];
           else if (need & (1u << k)) T[k] = sR[k * MAXT + tid];
+          if (T[k] != old) chg |= 1u << k;
         }
       }
       // no barrier here: the next sweep's solves change sT only after the
