@@ -457,8 +457,13 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
     }
     // vertices of this copy whose value changed in the previous sweep (all
     // on the first): a solve whose three inputs are unchanged returns what
-    // it returned before, which cannot lower its target again
-    unsigned chg = 0xFu;
+    // it returned before, which cannot lower its target again.  A check
+    // never uses its results for ghost targets, so it skips those solves.
+    unsigned chg = 0xFu, ghost = 0u;
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) ghost |= (idx[k] >= nvp ? 1u : 0u) << k;
+    }
 #pragma unroll 1
     for (int it = 0; it < niter; ++it) {
       if (it == niter - 1) {
@@ -474,10 +479,17 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         const float m012 = fminf(fminf(T[0], T[1]), T[2]), m013 = fminf(fminf(T[0], T[1]), T[3]);
         const float m023 = fminf(fminf(T[0], T[2]), T[3]), m123 = fminf(fminf(T[1], T[2]), T[3]);
         // apex k: the other three values all LARGENUM -> LARGENUM (as tet_solve)
-        if ((chg & 0xEu) && m123 < LN && m123 + 0.999f * hgt[0] < T[0]) need |= 1u;
-        if ((chg & 0xDu) && m023 < LN && m023 + 0.999f * hgt[1] < T[1]) need |= 2u;
-        if ((chg & 0xBu) && m013 < LN && m013 + 0.999f * hgt[2] < T[2]) need |= 4u;
-        if ((chg & 0x7u) && m012 < LN && m012 + 0.999f * hgt[3] < T[3]) need |= 8u;
+        const unsigned allow = CHECK ? (~ghost & 0xFu) : 0xFu;  // checks: owned targets only
+        unsigned cand = 0u;
+        if (chg & 0xEu) cand |= 1u;
+        if (chg & 0xDu) cand |= 2u;
+        if (chg & 0xBu) cand |= 4u;
+        if (chg & 0x7u) cand |= 8u;
+        cand &= allow;
+        if ((cand & 1u) && m123 < LN && m123 + 0.999f * hgt[0] < T[0]) need |= 1u;
+        if ((cand & 2u) && m023 < LN && m023 + 0.999f * hgt[1] < T[1]) need |= 2u;
+        if ((cand & 4u) && m013 < LN && m013 + 0.999f * hgt[2] < T[2]) need |= 4u;
+        if ((cand & 8u) && m012 < LN && m012 + 0.999f * hgt[3] < T[3]) need |= 8u;
         const int n = __popc(need);
         if (n) {
           int pos = atomicAdd(&s_n[it & 1], n);
@@ -1139,8 +1151,9 @@ cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float 
 // Block size classes: patches of up to 384 element copies run 2, 3 or 4
 // CTAs per SM (registers capped at 85 / 56 / 42; StepParams::ctas), larger
 // ones one CTA of 512 or 1024 threads.
-// dynamic shared memory of k_fim_compact<MAXT>: slab + owned snapshot
-// (rounded up to 16 bytes), then 23 floats, one ushort4 and 4 ints per thread
+// dynamic shared memory of k_fim_compact<MAXT>: slab values and owned
+// snapshot (rounded up to 16 bytes), then 23 floats, one ushort4 and 4 ints
+// per thread
 inline int compact_smem(const StepParams& sp, int maxt) {
   return (int)sizeof(float) * (((2 * sp.lvp + sp.lgp + 3) & ~3) + 23 * maxt) + 8 * maxt + 16 * maxt;
 }
