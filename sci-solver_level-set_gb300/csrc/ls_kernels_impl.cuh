@@ -457,8 +457,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
     }
     // vertices of this copy whose value changed in the previous sweep (all
     // on the first): a solve whose three inputs are unchanged returns what
-    // it returned before, which cannot lower its target again.  A check
-    // never uses its results for ghost targets, so it skips those solves.
+    // it returned before, which cannot lower its target again.
     unsigned chg = 0xFu, ghost = 0u;
     if (act) {
 #pragma unroll
@@ -479,7 +478,9 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         const float m012 = fminf(fminf(T[0], T[1]), T[2]), m013 = fminf(fminf(T[0], T[1]), T[3]);
         const float m023 = fminf(fminf(T[0], T[2]), T[3]), m123 = fminf(fminf(T[1], T[2]), T[3]);
         // apex k: the other three values all LARGENUM -> LARGENUM (as tet_solve)
-        const unsigned allow = CHECK ? (~ghost & 0xFu) : 0xFu;  // checks: owned targets only
+        // a ghost target's result is only read by later sweeps of the same
+        // visit: the last sweep (and a check's only sweep) skips those solves
+        const unsigned allow = (it == niter - 1) ? (~ghost & 0xFu) : 0xFu;
         unsigned cand = 0u;
         if (chg & 0xEu) cand |= 1u;
         if (chg & 0xDu) cand |= 2u;
