@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
 // then run the listed solves densely, one solve per thread at a time.
 // Shared memory per CTA (stride MAXT): metric [11], heights [4], copy
 // values at the sweep start [4], ghost results [4], connectivity, list.
-template <int MAXT, int MINB>
+template <int MAXT, int MINB, bool PREC>
 __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState s, StepParams sp, int cur,
                                                             int check) {
   const bool CHECK = check != 0;
@@ -404,6 +404,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   float* sR = sTc + 4 * MAXT;             // [4][MAXT] results for ghost targets
   ushort4* sC = reinterpret_cast<ushort4*>(sR + 4 * MAXT);  // [MAXT] connectivity
   int* sItem = reinterpret_cast<int*>(sC + MAXT);           // [4 * MAXT] listed solves (copy << 2 | k)
+  int* sRep = sItem + 4 * MAXT;  // precision form: [4 * MAXT] solves to repeat in FP64
+  __shared__ int s_rep;
   __shared__ unsigned s_min;
   __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
@@ -422,7 +424,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  if (tid == 0) s_n[0] = s_n[1] = 0;
+  if (tid == 0) { s_n[0] = s_n[1] = 0; s_rep = 0; }
+  int nflag = 0;
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
     const int p = list[li];
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
@@ -518,9 +521,14 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
         else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
         else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
-        bool d = false;
-        const float r = tet_solve<float, false, false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.eps_h64,
-                                                       sp.largenum, 0.f, d);
+        bool ill = false;
+        const float r = tet_solve<float, false, PREC>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.eps_h64,
+                                                      sp.largenum, sp.tau, ill, own);
+        if (PREC && ill) {
+          // discriminant cancelled: repeat in FP64 after this pass, densely
+          sRep[atomicAdd(&s_rep, 1)] = code;
+          continue;
+        }
         const float nw = fminf(own, r);
         const ushort4 cv = sC[cc];
         const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
@@ -528,6 +536,26 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         else sR[k * MAXT + cc] = nw;
       }
       __syncthreads();
+      if constexpr (PREC) {
+        const int nrep = s_rep;
+        for (int i = tid; i < nrep; i += blockDim.x) {
+          const int code = sRep[i];
+          const int cc = code >> 2, k = code & 3;
+          float Mq[11], Tq[4];
+#pragma unroll
+          for (int j = 0; j < 11; ++j) Mq[j] = sM[j * MAXT + cc];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) Tq[j] = sTc[j * MAXT + cc];
+          const float nw = fminf(Tq[k], solve_k_fp64(Mq, Tq, k, sp.eps_h64, sp.largenum));
+          const ushort4 cv = sC[cc];
+          const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
+          if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(nw));
+          else sR[k * MAXT + cc] = nw;
+          nflag++;
+        }
+        __syncthreads();
+        if (tid == 0) s_rep = 0;
+      }
       if (act) {
         chg = 0u;
 #pragma unroll
@@ -574,6 +602,10 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       }
     }
     __syncthreads();
+  }
+  if (PREC) {
+    nflag = __reduce_add_sync(0xffffffffu, nflag);
+    if ((tid & 31) == 0 && nflag) atomicAdd(&s.stats[6], (unsigned long long)nflag);
   }
 }
 
@@ -1153,10 +1185,10 @@ cudaError_t launch_seed(const DevMesh& m, const DevState& s, int use_all, float 
 // CTAs per SM (registers capped at 85 / 56 / 42; StepParams::ctas), larger
 // ones one CTA of 512 or 1024 threads.
 // dynamic shared memory of k_fim_compact<MAXT>: slab values and owned
-// snapshot (rounded up to 16 bytes), then 23 floats, one ushort4 and 4 ints
-// per thread
+// snapshot (rounded up to 16 bytes), then 23 floats, one ushort4 and 8 ints
+// (listed solves, FP64 repeats) per thread
 inline int compact_smem(const StepParams& sp, int maxt) {
-  return (int)sizeof(float) * (((2 * sp.lvp + sp.lgp + 3) & ~3) + 23 * maxt) + 8 * maxt + 16 * maxt;
+  return (int)sizeof(float) * (((2 * sp.lvp + sp.lgp + 3) & ~3) + 23 * maxt) + 8 * maxt + 32 * maxt;
 }
 
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
@@ -1174,17 +1206,24 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
     if (xd) { if (pr) LS_FIM(4, T, true, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, true, B, false); } \
     else { if (pr) LS_FIM(4, T, false, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, false, B, false); } \
   } while (0)
-  if (kLbSkip && m.dim == 3 && !pr) {
+  if (kLbSkip && m.dim == 3 && pr) {
+    // fast build, tetrahedra, precision form: compacted solves, FP64 repeats
+    // run densely after each sweep's FP32 pass
+    const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
+    if (L.fim_block <= 384) k_fim_compact<384, 2, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+    else if (L.fim_block <= 512) k_fim_compact<512, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+    else k_fim_compact<1024, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+  } else if (kLbSkip && m.dim == 3) {
     // fast build, tetrahedra: compacted solves
     const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
     if (L.fim_block <= 384) {
-      if (sp.ctas == 2) k_fim_compact<384, 2><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
-      else if (sp.ctas == 4) k_fim_compact<384, 4><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
-      else k_fim_compact<384, 3><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      if (sp.ctas == 2) k_fim_compact<384, 2, false><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      else if (sp.ctas == 4) k_fim_compact<384, 4, false><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      else k_fim_compact<384, 3, false><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     } else if (L.fim_block <= 512) {
-      k_fim_compact<512, 1><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      k_fim_compact<512, 1, false><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     } else {
-      k_fim_compact<1024, 1><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+      k_fim_compact<1024, 1, false><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     }
   } else if (m.dim == 3) {
     if (L.fim_block <= 384) {
@@ -1256,20 +1295,29 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
     const int maxt = L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024;
     const int cs = compact_smem(sp, maxt);
     if (L.fim_block <= 384 && sp.ctas == 2) {
-      e = cudaFuncSetAttribute(k_fim_compact<384, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 2>, L.fim_block, cs);
+      e = cudaFuncSetAttribute(k_fim_compact<384, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 2, false>, L.fim_block, cs);
     } else if (L.fim_block <= 384 && sp.ctas == 4) {
-      e = cudaFuncSetAttribute(k_fim_compact<384, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 4>, L.fim_block, cs);
+      e = cudaFuncSetAttribute(k_fim_compact<384, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 4, false>, L.fim_block, cs);
     } else if (L.fim_block <= 384) {
-      e = cudaFuncSetAttribute(k_fim_compact<384, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 3>, L.fim_block, cs);
+      e = cudaFuncSetAttribute(k_fim_compact<384, 3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 3, false>, L.fim_block, cs);
     } else if (L.fim_block <= 512) {
-      e = cudaFuncSetAttribute(k_fim_compact<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<512, 1>, L.fim_block, cs);
+      e = cudaFuncSetAttribute(k_fim_compact<512, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<512, 1, false>, L.fim_block, cs);
     } else {
-      e = cudaFuncSetAttribute(k_fim_compact<1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
-      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<1024, 1>, L.fim_block, cs);
+      e = cudaFuncSetAttribute(k_fim_compact<1024, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<1024, 1, false>, L.fim_block, cs);
+    }
+    // precision-form variants (selected at launch when tau > 0)
+    if (e == cudaSuccess) {
+      if (L.fim_block <= 384)
+        e = cudaFuncSetAttribute(k_fim_compact<384, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      else if (L.fim_block <= 512)
+        e = cudaFuncSetAttribute(k_fim_compact<512, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+      else
+        e = cudaFuncSetAttribute(k_fim_compact<1024, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     }
   } else if (m.dim == 3) {
     if (L.fim_block <= 384 && sp.ctas == 2)
