@@ -441,7 +441,7 @@ def main():
                     + ps["ms_update"])
     kernel_ms = {k: ps["ms_" + k] / prof_steps for k in ("sweep", "check", "schedule", "seed", "narrowband", "update")}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profile_traffic(), "kernel": "k_fim (FIM patch sweep launches)",
+                "traffic": profile_traffic(), "kernel": "k_fim_compact (FIM patch sweep launches)",
                 "peak_source": peak_kind,
                 "share_of_step": (ps["ms_sweep"] / step_ms_prof) if step_ms_prof > 0 else None,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": sweep_ms}
