@@ -276,6 +276,103 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   return TD;
 }
 
+// The same tet update with predicated candidates instead of branches (fast
+// build): every quadratic's roots and candidate distances are evaluated and
+// the invalid ones masked, so the lanes of a warp stay converged through the
+// solve.  Valid candidates use the same expressions as tet_solve.
+__device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
+                                                float BCBC, float BCCD, float CDCD, float eps_h, float LN) {
+  if (TA >= LN && TB >= LN && TC >= LN) return LN;
+  float FaceTAC = LN, FaceTAB = LN, FaceTBC = LN, TD = LN;
+  const float TAC = TC - TA, TBC = TC - TB, TAB = TB - TA;
+  float p, q, r, delta;
+  // face BC (lambda1 = 0)
+  p = BCBC * TBC * TBC - BCBC * BCBC;
+  q = (BCCD + BCCD) * TBC * TBC - 2.f * BCBC * BCCD;
+  r = TBC * TBC * CDCD - BCCD * BCCD;
+  delta = q * q - 4.f * p * r;
+  {
+    const bool ok = delta >= 0.f;
+    const float sq = sqrtf(fmaxf(delta, 0.f));
+#pragma unroll
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const float l2 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l3 = 1.f - l2;
+      const float c = TB * l2 + TC * l3 + sqrtf(fmaxf((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD), 0.f));
+      if (ok && l2 >= 0.f && l2 <= 1.f) FaceTBC = fminf(FaceTBC, c);
+    }
+  }
+  FaceTBC = fminf(FaceTBC, fminf(TB + sqrtf((BCBC + BCCD) + (BCCD + CDCD)), TC + sqrtf(CDCD)));
+  // face AB (lambda3 = 0)
+  const float gammax = ACAC - ACBC, gammay = ACBC - BCBC, gammaz = ACCD - BCCD;
+  p = (TAB * TAB * ACAC - gammax * gammax) + (BCBC * TAB * TAB - gammay * gammay) -
+      ((ACBC + ACBC) * TAB * TAB - 2.f * gammax * gammay);
+  q = -(BCBC * TAB * TAB - gammay * gammay) * 2.f + ((ACBC + ACBC) * TAB * TAB - 2.f * gammax * gammay) +
+      ((ACCD + ACCD) * TAB * TAB - 2.f * gammax * gammaz) - ((BCCD + BCCD) * TAB * TAB - 2.f * gammay * gammaz);
+  r = (TAB * TAB * BCBC - gammay * gammay) + ((BCCD + BCCD) * TAB * TAB - 2.f * gammay * gammaz) +
+      (TAB * TAB * CDCD - gammaz * gammaz);
+  delta = q * q - 4.f * p * r;
+  {
+    const bool ok = delta >= 0.f;
+    const float sq = sqrtf(fmaxf(delta, 0.f));
+#pragma unroll
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const float l1 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l2 = 1.f - l1;
+      const float c = TA * l1 + TB * l2 +
+                      sqrtf(fmaxf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                                      (l1 * ACCD + l2 * BCCD + CDCD),
+                                  0.f));
+      if (ok && l1 >= 0.f && l1 <= 1.f) FaceTAB = fminf(FaceTAB, c);
+    }
+  }
+  FaceTAB = fminf(FaceTAB, fminf(TB + sqrtf((BCBC + BCCD) + (BCCD + CDCD)), TA + sqrtf((ACAC + ACCD) + (ACCD + CDCD))));
+  // face AC (lambda2 = 0)
+  p = ACAC * TAC * TAC - ACAC * ACAC;
+  q = (ACCD + ACCD) * TAC * TAC - 2.f * ACAC * ACCD;
+  r = TAC * TAC * CDCD - ACCD * ACCD;
+  delta = q * q - 4.f * p * r;
+  {
+    const bool ok = delta >= 0.f;
+    const float sq = sqrtf(fmaxf(delta, 0.f));
+#pragma unroll
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const float l1 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l3 = 1.f - l1;
+      const float c = TA * l1 + TC * l3 + sqrtf(fmaxf((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD), 0.f));
+      if (ok && l1 >= 0.f && l1 <= 1.f) FaceTAC = fminf(FaceTAC, c);
+    }
+  }
+  FaceTAC = fminf(FaceTAC, fminf(TA + sqrtf((ACAC + ACCD) + (ACCD + CDCD)), TC + sqrtf(CDCD)));
+  // interior of face ABC
+  const float s = TAC * ACBC - TBC * ACAC;
+  const float t = TAC * BCCD - TBC * ACCD;
+  const float h = -(TAC * BCBC - TBC * ACBC);
+  p = (TAC * TAC * ACAC - ACAC * ACAC) * h * h + (BCBC * TAC * TAC - ACBC * ACBC) * s * s +
+      ((ACBC + ACBC) * TAC * TAC - 2.f * ACAC * ACBC) * s * h;
+  q = (BCBC * TAC * TAC - ACBC * ACBC) * 2.f * s * t + ((ACBC + ACBC) * TAC * TAC - 2.f * ACAC * ACBC) * t * h +
+      ((ACCD + ACCD) * TAC * TAC - 2.f * ACAC * ACCD) * h * h + ((BCCD + BCCD) * TAC * TAC - 2.f * ACBC * ACCD) * s * h;
+  r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - 2.f * ACBC * ACCD) * t * h +
+      (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
+  delta = q * q - 4.f * p * r;
+  {
+    const bool ok = delta >= 0.f;
+    const float sq = sqrtf(fmaxf(delta, 0.f));
+#pragma unroll
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const float l1 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l2 = (s * l1 + t) / (h + eps_h);
+      const float l3 = 1.f - l1 - l2;
+      const float c = TA * l1 + TB * l2 + TC * l3 +
+                      sqrtf(fmaxf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                                      (l1 * ACCD + l2 * BCCD + CDCD),
+                                  0.f));
+      if (ok && l1 >= 0.f && l1 <= 1.f && l2 >= 0.f && l2 <= 1.f && l3 >= 0.f && l3 <= 1.f) TD = fminf(TD, c);
+    }
+  }
+  return fminf(TD, fminf(FaceTBC, fminf(FaceTAB, FaceTAC)));
+}
+
 // Triangle update of C from edge AB (speed 1); the square roots are taken in
 // single precision as in the reference, which passes doubles to sqrtf.
 template <typename R>

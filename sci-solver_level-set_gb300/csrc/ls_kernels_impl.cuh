@@ -522,8 +522,12 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
         else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
         bool ill = false;
-        const float r = tet_solve<float, false, PREC>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.eps_h64,
-                                                      sp.largenum, sp.tau, ill, own);
+        float r;
+        if constexpr (PREC)
+          r = tet_solve<float, false, true>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.eps_h64, sp.largenum,
+                                            sp.tau, ill, own);
+        else
+          r = tet_solve_pred(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum);
         if (PREC && ill) {
           // discriminant cancelled: repeat in FP64 after this pass, densely
           sRep[atomicAdd(&s_rep, 1)] = code;
