@@ -87,7 +87,10 @@ typedef struct ls_params {
   int side_lengths;       /* sideLengths_      (1)    structured partition side       */
   double bandwidth;       /* bandwidth_        (16.0) */
   int metis_size;         /* metisSize_        (16)   target vertices per graph patch */
-  int partition_type;     /* partitionType_    (0)    0 graph, 1 structured blocks    */
+  int partition_type;     /* partitionType_    (0)    1 structured blocks; otherwise patches
+                           * of metis_size vertices: 2 recursive coordinate bisection,
+                           * any other value (the reference's METIS path) recursive
+                           * graph bisection (ls_partition_graph) */
   int verbose;            /* verbose_          (0)    */
   /* extensions */
   int update_kind;        /* LS_UPDATE_*       (ADVECT) */
@@ -248,12 +251,21 @@ ls_status ls_partition_structured(int dim, int nside, int block, int nv, int* np
  * recursive coordinate bisection into ceil(nv / target) parts (3D) or
  * max(2, nv / target) parts (2D, meshFIM2d.cu:380-382). */
 ls_status ls_partition_rcb(int dim, const float* xyz, int nv, int target, int* npart, int* nparts);
+/* Graph partition from the mesh connectivity alone (no counterpart in the
+ * reference, which calls METIS_PartGraphKway): recursive bisection of the
+ * vertex graph by breadth-first level structures from pseudo-peripheral
+ * vertices, then greedy boundary refinement that lowers the edge cut within
+ * a 3 % size tolerance; same part counts as ls_partition_rcb. */
+ls_status ls_partition_graph(int dim, const int* elems, int ne, int nv, int target, int* npart, int* nparts);
+/* Mesh edges whose vertices lie in different parts. */
+ls_status ls_edge_cut(int dim, const int* elems, int ne, int nv, const int* npart, long long* cut);
 
 /* Autotuner (no counterpart in the reference): times trial_steps steps (after
  * one warm-up step, from the handle's phi0) for each candidate patch size --
  * structured block side 2, 3, 4 (3D) / 4, 5, 6, 8 (2D) when
- * partition_type = 1, RCB target 8, 16, 27, 32, 64 (3D) / 16, 25, 36, 64
- * (2D) otherwise, or only the caller's partition when ls_set_partition was
+ * partition_type = 1, patch target size (metis_size) 8, 16, 27, 32, 64 (3D)
+ * / 16, 25, 36, 64 (2D) for the graph and RCB partitioners, or only the
+ * caller's partition when ls_set_partition was
  * used -- and each FIM CTAs-per-SM setting (2, 3, 4; patches of up to 384
  * element copies), picks the highest narrowband vertex-updates/s, writes it
  * into the handle's parameters (block_size or metis_size,

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblsgb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["ls_layout.cpp", "ls_meshio.cpp", "ls_api.cpp", "LevelSet.cpp", "ls_solver.cu", "ls_kernels.cu", "ls_kernels_exact.cu", "ls_noalloc.cu", "ls_mlp.cu"]
+SOURCES = ["ls_layout.cpp", "ls_meshio.cpp", "ls_partition.cpp", "ls_api.cpp", "LevelSet.cpp", "ls_solver.cu", "ls_kernels.cu", "ls_kernels_exact.cu", "ls_noalloc.cu", "ls_mlp.cu"]
 # translation units compiled without FMA contraction
 NO_FMA = {"ls_kernels_exact.cu"}
 # the fast kernel build: hardware-approximate division and square root

@@ -14,6 +14,7 @@
 #include "ls_layout.h"
 #include "ls_meshio.h"
 #include "ls_mlp.h"
+#include "ls_partition.h"
 #include "ls_solver.h"
 
 struct ls_handle {
@@ -310,6 +311,24 @@ ls_status ls_partition_structured(int dim, int nside, int block, int nv, int* np
   return LS_OK;
 }
 
+ls_status ls_partition_graph(int dim, const int* elems, int ne, int nv, int target, int* npart, int* nparts) {
+  if ((dim != 2 && dim != 3) || !elems || ne <= 0 || nv <= 0 || target <= 0 || !npart || !nparts)
+    return LS_BAD_INPUT;
+  const int d1 = dim + 1;
+  for (long long i = 0; i < (long long)ne * d1; ++i)
+    if (elems[i] < 0 || elems[i] >= nv) return LS_BAD_INPUT;
+  int np = dim == 3 ? (int)std::ceil((double)nv / target) : std::max(2, nv / target);
+  np = std::max(1, std::min(np, nv));
+  *nparts = lsgb::partition_graph(nv, elems, ne, d1, np, npart);
+  return LS_OK;
+}
+
+ls_status ls_edge_cut(int dim, const int* elems, int ne, int nv, const int* npart, long long* cut) {
+  if ((dim != 2 && dim != 3) || !elems || ne <= 0 || nv <= 0 || !npart || !cut) return LS_BAD_INPUT;
+  *cut = lsgb::edge_cut(nv, elems, ne, dim + 1, npart);
+  return LS_OK;
+}
+
 ls_status ls_partition_rcb(int dim, const float* xyz, int nv, int target, int* npart, int* nparts) {
   if ((dim != 2 && dim != 3) || !xyz || nv <= 0 || target <= 0 || !npart || !nparts) return LS_BAD_INPUT;
   int np = dim == 3 ? (int)std::ceil((double)nv / target) : std::max(2, nv / target);
@@ -330,8 +349,10 @@ ls_status ls_prepare(ls_handle* h) {
     ls_status s;
     if (h->prm.partition_type == 1)
       s = ls_partition_structured(dim, h->prm.side_lengths, h->prm.block_size, h->nv, h->npart.data(), &h->nparts);
-    else
+    else if (h->prm.partition_type == 2)
       s = ls_partition_rcb(dim, h->xyz.data(), h->nv, h->prm.metis_size, h->npart.data(), &h->nparts);
+    else  // the reference's METIS path: a graph partition of metis_size-vertex patches
+      s = ls_partition_graph(dim, h->elems.data(), h->ne, h->nv, h->prm.metis_size, h->npart.data(), &h->nparts);
     if (s != LS_OK) {
       h->npart.clear();
       return fail(h, s, "partitioning failed (structured partition needs side_lengths^dim vertices)");

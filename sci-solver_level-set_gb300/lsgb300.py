@@ -71,7 +71,7 @@ EXPORTS = [
     "ls_batch_get_layout", "ls_autotune", "ls_mlp_create", "ls_mlp_destroy", "ls_mlp_last_error",
     "ls_mlp_num_params", "ls_mlp_set_params", "ls_mlp_get_params", "ls_mlp_predict", "ls_mlp_gradients",
     "ls_mlp_train", "ls_mlp_reserve_pairs", "ls_mlp_clear_pairs", "ls_mlp_num_pairs", "ls_mlp_train_pairs",
-    "ls_learn_collect", "ls_set_learned",
+    "ls_learn_collect", "ls_set_learned", "ls_partition_graph", "ls_edge_cut",
 ]
 
 class TuneTrial(ctypes.Structure):
@@ -158,6 +158,8 @@ def lib():
     L.ls_version.restype = ctypes.c_char_p
     L.ls_partition_structured.argtypes = [I, I, I, I, V, ctypes.POINTER(I)]
     L.ls_partition_rcb.argtypes = [I, V, I, I, V, ctypes.POINTER(I)]
+    L.ls_partition_graph.argtypes = [I, V, I, I, I, V, ctypes.POINTER(I)]
+    L.ls_edge_cut.argtypes = [I, V, I, I, V, ctypes.POINTER(ctypes.c_longlong)]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("ls_last_error", "ls_version", "ls_batch_last_error", "ls_mlp_last_error"):
@@ -201,6 +203,26 @@ def partition_rcb(dim, xyz, target):
     if rc:
         raise LevelSetError(rc, "rcb partition")
     return npart, n.value
+
+
+def partition_graph(dim, elems, nv, target):
+    el = np.ascontiguousarray(elems, np.int32)
+    npart = np.zeros(nv, np.int32)
+    n = ctypes.c_int(0)
+    rc = lib().ls_partition_graph(dim, _ptr(el), len(el), nv, target, _ptr(npart), ctypes.byref(n))
+    if rc:
+        raise LevelSetError(rc, "graph partition")
+    return npart, n.value
+
+
+def edge_cut(dim, elems, nv, npart):
+    el = np.ascontiguousarray(elems, np.int32)
+    a = np.ascontiguousarray(npart, np.int32)
+    cut = ctypes.c_longlong(0)
+    rc = lib().ls_edge_cut(dim, _ptr(el), len(el), nv, _ptr(a), ctypes.byref(cut))
+    if rc:
+        raise LevelSetError(rc, "edge cut")
+    return cut.value
 
 
 class LevelSet:
