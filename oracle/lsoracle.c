@@ -66,8 +66,9 @@ static float root_b(float p, float q, float r, float delta) { return r / stable_
  * fall below `cutoff` (the target's current value) is skipped -- every
  * candidate is at least min(TA, TB, TC) plus D's height over the plane ABC
  * (Gram determinants of AC, BC, CD; taken x 0.999); otherwise a quadratic
- * whose discriminant cancels flags the solve for an FP64 repeat, and the
- * quadratic roots are taken in the cancellation-free form. */
+ * whose arrival times are all below LN and whose discriminant cancels flags
+ * the solve for an FP64 repeat, and the quadratic roots are taken in the
+ * cancellation-free form. */
 static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
                           float ACCD, float BCBC, float BCCD, float CDCD,
                           double eps_h, float LN, float tau, int* ill, int fdiv, float cutoff) {
@@ -89,7 +90,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   q = (BCCD + BCCD) * TBC * TBC - 2 * BCBC * BCCD;
   r = TBC * TBC * CDCD - BCCD * BCCD;
   delta = q * q - 4 * p * r;
-  if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
+  if (ill && fmaxf(TB, TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
     lambda1 = 0.0f;
     lambda2 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
@@ -117,7 +118,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   r = (TAB * TAB * BCBC - gammay * gammay) + ((BCCD + BCCD) * TAB * TAB - 2 * gammay * gammaz) +
       (TAB * TAB * CDCD - gammaz * gammaz);
   delta = q * q - 4 * p * r;
-  if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
+  if (ill && fmaxf(TA, TB) < LN && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
     lambda1 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = 1 - lambda1;
@@ -143,7 +144,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   q = (ACCD + ACCD) * TAC * TAC - 2 * ACAC * ACCD;
   r = TAC * TAC * CDCD - ACCD * ACCD;
   delta = q * q - 4 * p * r;
-  if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
+  if (ill && fmaxf(TA, TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
     lambda1 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = 0.0f;
@@ -173,7 +174,7 @@ static float tet_f32_impl(float TA, float TB, float TC, float ACAC, float ACBC,
   r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - 2 * ACBC * ACCD) * t * h +
       (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
   delta = q * q - 4 * p * r;
-  if (ill && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
+  if (ill && fmaxf(fmaxf(TA, TB), TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4 * p * r))) *ill = 1;
   if (delta >= 0.0) {
     lambda1 = ill ? root_a(p, q, r, delta) : (float)((double)(-q + sqrtf(delta)) / (2.0 * (double)p));
     lambda2 = fdiv ? (s * lambda1 + t) / (h + (float)eps_h)

@@ -110,6 +110,8 @@ enum { LS_FAR = 0, LS_ACTIVE = 1 };
 
 template <typename R>
 __device__ __forceinline__ R rmin(R a, R b) { return fmin(a, b); }
+template <typename R>
+__device__ __forceinline__ R rmax(R a, R b) { return fmax(a, b); }
 template <>
 __device__ __forceinline__ float rmin<float>(float a, float b) { return fminf(a, b); }
 
@@ -147,6 +149,10 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
                                        R CDCD, R eps_h, double eps_h64, R LN, R tau, bool& ill,
                                        R cutoff = R(0)) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
+  // precision form (CHK): a quadratic is flagged only when all its arrival
+  // times are below LARGENUM -- with one at LARGENUM its candidates lie at or
+  // above the edge candidates computed separately (equal values, e.g. two
+  // LARGENUMs, make the discriminant vanish identically)
   if (CHK || LB) {
     // precision form: a solve whose candidates cannot fall below `cutoff`
     // (the target's current value) is skipped -- every candidate is at
@@ -168,7 +174,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   q = (BCCD + BCCD) * TBC * TBC - two * BCBC * BCCD;
   r = TBC * TBC * CDCD - BCCD * BCCD;
   delta = q * q - four * p * r;
-  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK && rmax(TB, TC) < LN) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
     R ra, rb;
@@ -198,7 +204,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   r = (TAB * TAB * BCBC - gammay * gammay) + ((BCCD + BCCD) * TAB * TAB - two * gammay * gammaz) +
       (TAB * TAB * CDCD - gammaz * gammaz);
   delta = q * q - four * p * r;
-  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK && rmax(TA, TB) < LN) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
     R ra, rb;
@@ -222,7 +228,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   q = (ACCD + ACCD) * TAC * TAC - two * ACAC * ACCD;
   r = TAC * TAC * CDCD - ACCD * ACCD;
   delta = q * q - four * p * r;
-  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK && rmax(TA, TC) < LN) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
     R ra, rb;
@@ -250,7 +256,7 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
   r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - two * ACBC * ACCD) * t * h +
       (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
   delta = q * q - four * p * r;
-  if (CHK) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
+  if (CHK && rmax(rmax(TA, TB), TC) < LN) ill |= (fabs(delta) <= tau * (q * q + fabs(four * p * r)));
   if (delta >= zero) {
     const R sq = sqrt(delta);
     R ra, rb;

@@ -106,26 +106,26 @@ constexpr bool kLbSkip = false;
 constexpr bool kLbSkip = true;
 #endif
 
-template <int D1, bool XDIV, bool PREC>
+// The four solves of one element copy from the values at the sweep start
+// (Jacobi within the element), each kept only where it lowers its target.
+// Precision-form tets use solve_copy_flags and the deferred FP64 repeats
+// instead.
+template <int D1, bool XDIV>
 __device__ __forceinline__ void solve_copy(const float* Mt, const float T[4], float out[4], float eps_h,
-                                           double eps_h64, float LN, float tau, int& nflag) {
+                                           double eps_h64, float LN) {
   if (D1 == 4) {
     const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4];
     const float CDCD = Mt[5], ADAD = Mt[6], ADBD = Mt[7], ADCD = Mt[8], BDBD = Mt[9], CDBD = Mt[10];
     const float TA = T[0], TB = T[1], TC = T[2], TD = T[3];
-    bool ill[4] = {false, false, false, false};
-    float r3 = tet_solve<float, XDIV, PREC, kLbSkip>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h, eps_h64, LN, tau, ill[3], TD);
-    float r0 = tet_solve<float, XDIV, PREC, kLbSkip>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h, eps_h64, LN, tau, ill[0], TA);
-    float r1 = tet_solve<float, XDIV, PREC, kLbSkip>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h, eps_h64, LN, tau, ill[1], TB);
-    float r2 = tet_solve<float, XDIV, PREC, kLbSkip>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h, eps_h64, LN, tau, ill[2], TC);
-    if (PREC && (ill[0] | ill[1] | ill[2] | ill[3])) {
-      const double L64 = LN;
-      bool d = false;
-      if (ill[3]) { r3 = (float)tet_solve<double, false, false>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-      if (ill[0]) { r0 = (float)tet_solve<double, false, false>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-      if (ill[1]) { r1 = (float)tet_solve<double, false, false>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-      if (ill[2]) { r2 = (float)tet_solve<double, false, false>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h64, eps_h64, L64, 0.0, d); nflag++; }
-    }
+    bool d = false;
+    const float r3 = tet_solve<float, XDIV, false, kLbSkip>(TA, TB, TC, ACAC, ACBC, ACCD, BCBC, BCCD, CDCD, eps_h,
+                                                           eps_h64, LN, 0.f, d, TD);
+    const float r0 = tet_solve<float, XDIV, false, kLbSkip>(TB, TD, TC, BCBC, -BCCD, -ACBC, CDCD, ACCD, ACAC, eps_h,
+                                                           eps_h64, LN, 0.f, d, TA);
+    const float r1 = tet_solve<float, XDIV, false, kLbSkip>(TA, TD, TC, ACAC, -ACCD, -ACBC, CDCD, BCCD, BCBC, eps_h,
+                                                           eps_h64, LN, 0.f, d, TB);
+    const float r2 = tet_solve<float, XDIV, false, kLbSkip>(TA, TB, TD, ADAD, ADBD, -ADCD, BDBD, -CDBD, CDCD, eps_h,
+                                                           eps_h64, LN, 0.f, d, TC);
     out[3] = fminf(TD, r3);
     out[0] = fminf(TA, r0);
     out[1] = fminf(TB, r1);
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
             nw[k] = fminf(T[k], rr[k]);
           }
         } else {
-          solve_copy<D1, XDIV, PREC>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum, sp.tau, nflag);
+          solve_copy<D1, XDIV>(Mt, T, nw, sp.eps_h, sp.eps_h64, sp.largenum);
         }
 #pragma unroll
         for (int k = 0; k < D1; ++k) {
