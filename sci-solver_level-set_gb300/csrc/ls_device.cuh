@@ -285,9 +285,13 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
 // The same tet update with predicated candidates instead of branches (fast
 // build): every quadratic's roots and candidate distances are evaluated and
 // the invalid ones masked, so the lanes of a warp stay converged through the
-// solve.  Valid candidates use the same expressions as tet_solve.
+// solve.  Valid candidates use the same expressions as tet_solve; CHK adds
+// the precision form's flags and cancellation-free roots (as tet_solve with
+// CHK, without its lower-bound skip, which the caller has applied).
+template <bool CHK = false>
 __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
-                                                float BCBC, float BCCD, float CDCD, float eps_h, float LN) {
+                                                float BCBC, float BCCD, float CDCD, float eps_h, float LN,
+                                                float tau = 0.f, bool* ill = nullptr) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
   float FaceTAC = LN, FaceTAB = LN, FaceTBC = LN, TD = LN;
   const float TAC = TC - TA, TBC = TC - TB, TAB = TB - TA;
@@ -297,12 +301,15 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   q = (BCCD + BCCD) * TBC * TBC - 2.f * BCBC * BCCD;
   r = TBC * TBC * CDCD - BCCD * BCCD;
   delta = q * q - 4.f * p * r;
+  if (CHK && fmaxf(TB, TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
     const bool ok = delta >= 0.f;
     const float sq = sqrtf(fmaxf(delta, 0.f));
+    float ra, rb;
+    roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      const float l2 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l2 = sgn ? rb : ra;
       const float l3 = 1.f - l2;
       const float c = TB * l2 + TC * l3 + sqrtf(fmaxf((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD), 0.f));
       if (ok && l2 >= 0.f && l2 <= 1.f) FaceTBC = fminf(FaceTBC, c);
@@ -318,12 +325,15 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   r = (TAB * TAB * BCBC - gammay * gammay) + ((BCCD + BCCD) * TAB * TAB - 2.f * gammay * gammaz) +
       (TAB * TAB * CDCD - gammaz * gammaz);
   delta = q * q - 4.f * p * r;
+  if (CHK && fmaxf(TA, TB) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
     const bool ok = delta >= 0.f;
     const float sq = sqrtf(fmaxf(delta, 0.f));
+    float ra, rb;
+    roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      const float l1 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l1 = sgn ? rb : ra;
       const float l2 = 1.f - l1;
       const float c = TA * l1 + TB * l2 +
                       sqrtf(fmaxf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
@@ -338,12 +348,15 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   q = (ACCD + ACCD) * TAC * TAC - 2.f * ACAC * ACCD;
   r = TAC * TAC * CDCD - ACCD * ACCD;
   delta = q * q - 4.f * p * r;
+  if (CHK && fmaxf(TA, TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
     const bool ok = delta >= 0.f;
     const float sq = sqrtf(fmaxf(delta, 0.f));
+    float ra, rb;
+    roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      const float l1 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l1 = sgn ? rb : ra;
       const float l3 = 1.f - l1;
       const float c = TA * l1 + TC * l3 + sqrtf(fmaxf((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD), 0.f));
       if (ok && l1 >= 0.f && l1 <= 1.f) FaceTAC = fminf(FaceTAC, c);
@@ -361,12 +374,15 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   r = (TAC * TAC * BCBC - ACBC * ACBC) * t * t + ((BCCD + BCCD) * TAC * TAC - 2.f * ACBC * ACCD) * t * h +
       (TAC * TAC * CDCD - ACCD * ACCD) * h * h;
   delta = q * q - 4.f * p * r;
+  if (CHK && fmaxf(fmaxf(TA, TB), TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
     const bool ok = delta >= 0.f;
     const float sq = sqrtf(fmaxf(delta, 0.f));
+    float ra, rb;
+    roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      const float l1 = (-q + (sgn ? -sq : sq)) / (2.f * p);
+      const float l1 = sgn ? rb : ra;
       const float l2 = (s * l1 + t) / (h + eps_h);
       const float l3 = 1.f - l1 - l2;
       const float c = TA * l1 + TB * l2 + TC * l3 +

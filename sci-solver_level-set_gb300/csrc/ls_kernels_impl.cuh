@@ -524,10 +524,9 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         bool ill = false;
         float r;
         if constexpr (PREC)
-          r = tet_solve<float, false, true>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.eps_h64, sp.largenum,
-                                            sp.tau, ill, own);
+          r = tet_solve_pred<true>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum, sp.tau, &ill);
         else
-          r = tet_solve_pred(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum);
+          r = tet_solve_pred<false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum);
         if (PREC && ill) {
           // discriminant cancelled: repeat in FP64 after this pass, densely
           sRep[atomicAdd(&s_rep, 1)] = code;
