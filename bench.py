@@ -325,7 +325,7 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="cells per side (128 = the benchmark workload)")
     ap.add_argument("--fp64-flagged", action="store_true", help="precision form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 0 = library default)")
+    ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 5 = two element copies per thread; 0 = library default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep 3x3x3-vertex patches and the default FIM CTAs per SM instead of the autotuner's pick")
     ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5"],

@@ -103,7 +103,9 @@ typedef struct ls_params {
   double length_scale;    /* FIM length unit when not LS_REF_COMPAT (0 -> mean edge length) */
   double fp64_threshold;  /* LS_FP64_FLAGGED: discriminant cancellation threshold tau (0 -> 2^-18) */
   int graph_chunk;        /* FIM iterations per loop body of the step graph (0 -> 4, rounded up to even) */
-  int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 (0 -> 3) */
+  int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 with one element copy
+                             per thread; 5: two copies per thread (fast build, tetrahedra; others run 3)
+                             (0 -> 5) */
 } ls_params;
 
 typedef struct ls_stats {

@@ -133,7 +133,7 @@ lsgb::SolverConfig solver_config(const ls_params& p) {
   cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
   cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;
   cfg.graph_chunk = p.graph_chunk > 0 ? p.graph_chunk : 4;
-  cfg.fim_ctas = p.fim_ctas_per_sm > 0 ? p.fim_ctas_per_sm : 3;
+  cfg.fim_ctas = p.fim_ctas_per_sm > 0 ? p.fim_ctas_per_sm : 5;
   cfg.dt = p.time_step;
   cfg.bandwidth = p.bandwidth;
   cfg.curv_coeff = p.curv_coeff;
@@ -171,7 +171,7 @@ ls_status ls_default_params(ls_params* p) {
   p->length_scale = 0.0;
   p->fp64_threshold = 3.814697265625e-06;
   p->graph_chunk = 4;
-  p->fim_ctas_per_sm = 3;
+  p->fim_ctas_per_sm = 5;
   return LS_OK;
 }
 
@@ -489,7 +489,8 @@ ls_status ls_autotune(ls_handle* h, int trial_steps, ls_tune_report* rep) {
   if (h->user_partition) sizes.push_back(0);
   else if (structured) sizes = (h->is_tri ? std::vector<int>{4, 5, 6, 8} : std::vector<int>{2, 3, 4});
   else sizes = (h->is_tri ? std::vector<int>{16, 25, 36, 64} : std::vector<int>{8, 16, 27, 32, 64});
-  const std::vector<int> ctas = {2, 3, 4};
+  // 2-4: one element copy per thread; 5: two per thread (tetrahedra only)
+  const std::vector<int> ctas = h->is_tri ? std::vector<int>{2, 3, 4} : std::vector<int>{2, 3, 4, 5};
   const ls_params saved = h->prm;
   struct Trial { int size, ctas; double ms, rate; };
   std::vector<Trial> trials;

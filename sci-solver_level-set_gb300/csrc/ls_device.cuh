@@ -85,7 +85,7 @@ struct StepParams {
   float scale;       // FIM frame length unit (1 with the reference's semantics)
   float tau;         // precision form: discriminant cancellation threshold
   int xdiv;          // interior division in double (bit-exact build, reference semantics)
-  int ctas;          // FIM CTAs per SM for patches of up to 384 copies (2, 3 or 4)
+  int ctas;          // FIM CTAs per SM for patches of up to 384 copies (2, 3, 4; 5: two copies per thread)
   float tol;       // convergence threshold on oldT - newT
   float eps_h;     // denominator offset of the interior tet update
   double eps_h64;

@@ -612,6 +612,218 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   }
 }
 
+// Fast-build FIM patch visit for tetrahedra, two element copies per thread.
+// The same sweep as k_fim_compact (listing with the lower bound, the
+// unchanged-input and unread-ghost skips; dense predicated solves; per-vertex
+// minimum; private ghost values) with each copy's carried state in shared
+// memory instead of registers, so that a patch of up to 384 copies runs on
+// at most 192 threads and five patches are resident per SM (the one-copy
+// kernel fits three): the CTA barriers between the listing, solve and
+// refresh phases then leave fewer issue slots idle.  Shared memory per CTA
+// (ncap = the largest patch's copies, at most 2 x blockDim): copy values
+// float4 [ncap] (carried across sweeps), metric float4 [3][ncap] (11 terms,
+// copy-major), heights float4 [ncap], ghost results float4 [ncap],
+// connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k),
+// flags uchar [ncap] (changed vertices in bits 0-3, ghost vertices in bits
+// 4-7).
+template <int MINB>
+__global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+  const bool CHECK = check != 0;
+  extern __shared__ float4 smem4[];
+  float* sT = reinterpret_cast<float*>(smem4);  // owned + ghost values
+  float* sOld = sT + sp.lvp + sp.lgp;          // owned values at the start of the last sweep
+  const int ncap = sp.lep;
+  float4* sTc = smem4 + (((2 * sp.lvp + sp.lgp + 3) & ~3) >> 2);
+  float4* sM = sTc + ncap;
+  float4* sH = sM + 3 * ncap;
+  float4* sR = sH + ncap;
+  ushort4* sC = reinterpret_cast<ushort4*>(sR + ncap);
+  unsigned short* sItem = reinterpret_cast<unsigned short*>(sC + ncap);
+  unsigned char* sF = reinterpret_cast<unsigned char*>(sItem + 4 * ncap);
+  __shared__ unsigned s_min;
+  __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
+  const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
+  const int count = CHECK ? s.counts[2] : s.counts[cur];
+  const int nxt = cur ^ 1;
+  int* nlist = nxt ? s.list1 : s.list0;
+  if (!CHECK && blockIdx.x == 0 && threadIdx.x == 0) {
+    s.counts[nxt] = 0;
+    s.counts[2] = 0;
+    if (count > 0) {
+      s.counts[4] += 1;
+      atomicAdd(&s.stats[5], 1ull);
+    }
+    atomicAdd(&s.stats[0], (unsigned long long)count);
+  }
+  if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
+  const int niter = CHECK ? 1 : sp.niter;
+  const int tid = threadIdx.x;
+  if (tid == 0) { s_n[0] = s_n[1] = 0; }
+  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+    const int p = list[li];
+    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+    const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
+    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+    for (int i = tid; i < nvp + ngp; i += blockDim.x)
+      sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
+    if (tid == 0) s_min = 0x7f800000u;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int c = tid + j * blockDim.x;
+      if (c < nep) {
+        const ushort4 cv = m.conn[es + c];
+        sC[c] = cv;
+        sTc[c] = make_float4(sT[cv.x], sT[cv.y], sT[cv.z], sT[cv.w]);
+        float Mt[11];
+        copy_metric<4>(m, (long long)es + c, Mt);
+        sM[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
+        sM[3 * c + 1] = make_float4(Mt[4], Mt[5], Mt[6], Mt[7]);
+        sM[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], 0.f);
+        const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
+        const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
+        const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
+                           ACCD * (ACBC * BCCD - BCBC * ACCD);
+        sH[c] = make_float4(sqrtf(fmaxf(det3 / (BCBC * CDCD - BCCD * BCCD), 0.f)),   // A over BCD
+                            sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f)),   // B over ACD
+                            sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f)),   // C over ABD
+                            sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f)));  // D over ABC
+        const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
+                               (cv.w >= nvp ? 8u : 0u);
+        sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
+      }
+    }
+    unsigned need[2] = {0u, 0u};
+#pragma unroll 1
+    for (int it = 0; it < niter; ++it) {
+      if (it == niter - 1) {
+        for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
+        __syncthreads();
+      }
+      // list this thread's solves that can lower their target (the tests of
+      // k_fim_compact)
+      const unsigned allow_ghost = (it == niter - 1) ? 0u : 0xFu;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int c = tid + j * blockDim.x;
+        need[j] = 0u;
+        if (c < nep) {
+          const float4 tv = sTc[c];
+          const float4 hv = sH[c];
+          const unsigned fl = sF[c];
+          const unsigned chg = fl & 0xFu, ghost = fl >> 4;
+          const float LN = sp.largenum;
+          const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
+          const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
+          unsigned cand = 0u;
+          if (chg & 0xEu) cand |= 1u;
+          if (chg & 0xDu) cand |= 2u;
+          if (chg & 0xBu) cand |= 4u;
+          if (chg & 0x7u) cand |= 8u;
+          cand &= (~ghost | allow_ghost) & 0xFu;
+          unsigned nd = 0u;
+          if ((cand & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
+          if ((cand & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
+          if ((cand & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
+          if ((cand & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
+          need[j] = nd;
+          const int n = __popc(nd);
+          if (n) {
+            int pos = atomicAdd(&s_n[it & 1], n);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
+          }
+        }
+      }
+      __syncthreads();
+      const int nitems = s_n[it & 1];
+      // the other parity's counter is idle until the next sweep's listing,
+      // which starts after the barrier below
+      if (tid == 0) s_n[(it & 1) ^ 1] = 0;
+      for (int i = tid; i < nitems; i += blockDim.x) {
+        const int code = sItem[i];
+        const int cc = code >> 2, k = code & 3;
+        const float4 tv = sTc[cc];
+        const float4 m0 = sM[3 * cc], m1 = sM[3 * cc + 1], m2 = sM[3 * cc + 2];
+        const float TA = tv.x, TB = tv.y, TC = tv.z, TD = tv.w;
+        const float ACAC = m0.x, ACBC = m0.y, ACCD = m0.z, BCBC = m0.w, BCCD = m1.x, CDCD = m1.y;
+        const float ADAD = m1.z, ADBD = m1.w, ADCD = m2.x, BDBD = m2.y, CDBD = m2.z;
+        // the permuted arguments of solve k (solve_copy's four calls)
+        float a0, a1, a2, g0, g1, g2, g3, g4, g5, own;
+        if (k == 3) { a0 = TA; a1 = TB; a2 = TC; g0 = ACAC; g1 = ACBC; g2 = ACCD; g3 = BCBC; g4 = BCCD; g5 = CDCD; own = TD; }
+        else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
+        else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
+        else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
+        const float r = tet_solve_pred<false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum);
+        const float nw = fminf(own, r);
+        const ushort4 cv = sC[cc];
+        const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
+        if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(nw));
+        else reinterpret_cast<float*>(sR)[4 * cc + k] = nw;
+      }
+      __syncthreads();
+      // refresh this thread's copies: owned vertices from the per-vertex
+      // minimum, ghost vertices from this sweep's own result where solved
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int c = tid + j * blockDim.x;
+        if (c < nep) {
+          const float4 tv = sTc[c];
+          const float4 rv = sR[c];
+          const ushort4 cv = sC[c];
+          const unsigned nd = need[j];
+          float4 nv;
+          nv.x = cv.x < nvp ? sT[cv.x] : ((nd & 1u) ? rv.x : tv.x);
+          nv.y = cv.y < nvp ? sT[cv.y] : ((nd & 2u) ? rv.y : tv.y);
+          nv.z = cv.z < nvp ? sT[cv.z] : ((nd & 4u) ? rv.z : tv.z);
+          nv.w = cv.w < nvp ? sT[cv.w] : ((nd & 8u) ? rv.w : tv.w);
+          const unsigned chg = (nv.x != tv.x ? 1u : 0u) | (nv.y != tv.y ? 2u : 0u) | (nv.z != tv.z ? 4u : 0u) |
+                               (nv.w != tv.w ? 8u : 0u);
+          sTc[c] = nv;
+          sF[c] = (unsigned char)((sF[c] & 0xF0u) | chg);
+        }
+      }
+      // no barrier here: every thread refreshes only its own copies, and the
+      // next sweep's solves read them after the barrier that follows its
+      // listing
+    }
+    __syncthreads();
+    if (tid == 0) s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
+    int con = 1;
+    for (int i = tid; i < nvp; i += blockDim.x) {
+      const int v = vs + i;
+      const float nt = sT[i];
+      float outv;
+      if (!s.seed[v]) {
+        if (!CHECK) s.DT_out[v] = nt;
+        con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
+        outv = nt;
+      } else {
+        outv = s.DT[v];
+      }
+      if (!CHECK) atomicMin(&s_min, __float_as_uint(outv));
+    }
+    con = __syncthreads_and(con);
+    if (tid == 0) {
+      if (!CHECK) {
+        atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
+        s.bcon[p] = con;
+        s.bmin[p] = __uint_as_float(s_min);
+        s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
+      } else {
+        if (!con) {
+          const int pos = atomicAdd(&s.counts[nxt], 1);
+          nlist[pos] = p;
+        } else {
+          s.blabel[p] = LS_FAR;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Schedule of one FIM iteration: one warp per patch of the current list.
 __global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
   const int count = s.counts[cur];
@@ -1194,6 +1406,13 @@ inline int compact_smem(const StepParams& sp, int maxt) {
   return (int)sizeof(float) * (((2 * sp.lvp + sp.lgp + 3) & ~3) + 23 * maxt) + 8 * maxt + 32 * maxt;
 }
 
+// dynamic shared memory of k_fim_pair for `ncap` copies: slab values, then
+// per copy 4 float4 records + metric (48 B) + connectivity (8 B) + listed
+// solves (8 B) + flags (1 B)
+inline int pair_smem(const StepParams& sp, int ncap) {
+  return (int)sizeof(float) * ((2 * sp.lvp + sp.lgp + 3) & ~3) + ncap * (16 * 3 + 48 + 8 + 8 + 1);
+}
+
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
                          const Launch& L, cudaStream_t st) {
   const bool xd = sp.xdiv != 0;
@@ -1216,6 +1435,9 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
     if (L.fim_block <= 384) k_fim_compact<384, 2, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     else if (L.fim_block <= 512) k_fim_compact<512, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     else k_fim_compact<1024, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
+  } else if (kLbSkip && m.dim == 3 && L.pair_block > 0) {
+    // fast build, tetrahedra: compacted solves, two copies per thread
+    k_fim_pair<5><<<L.fim_grid, L.pair_block, pair_smem(sp, sp.lep), st>>>(m, s, sp, cur, c);
   } else if (kLbSkip && m.dim == 3) {
     // fast build, tetrahedra: compacted solves
     const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
@@ -1292,12 +1514,19 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   if (L.fim_block < 64) L.fim_block = 64;
   L.fim_smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
   int occ = 0;
+  L.pair_block = 0;
   if (kLbSkip && m.dim == 3) {
     // compacted kernel (fast build): opt in to its shared memory, size the
     // grid by its occupancy
     const int maxt = L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024;
     const int cs = compact_smem(sp, maxt);
-    if (L.fim_block <= 384 && sp.ctas == 2) {
+    if (L.fim_block <= 384 && sp.ctas == 5) {
+      // two copies per thread: ceil(lep / 2) threads, whole warps
+      L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;
+      const int ps = pair_smem(sp, sp.lep);
+      e = cudaFuncSetAttribute(k_fim_pair<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_pair<5>, L.pair_block, ps);
+    } else if (L.fim_block <= 384 && sp.ctas == 2) {
       e = cudaFuncSetAttribute(k_fim_compact<384, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
       if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 2, false>, L.fim_block, cs);
     } else if (L.fim_block <= 384 && sp.ctas == 4) {

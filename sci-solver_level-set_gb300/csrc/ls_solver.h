@@ -15,6 +15,7 @@ namespace lsgb {
 struct Launch {
   int sms;
   int fim_grid, fim_block, fim_smem;
+  int pair_block;  // threads of the two-copies-per-thread sweep kernel (0: not used)
   int upd_grid, upd_block, upd_smem;
   int seed_grid;
   int warp_grid;

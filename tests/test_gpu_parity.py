@@ -74,10 +74,11 @@ def test_bitexact_update_kinds(name, n, update):
 
 
 @pytest.mark.parametrize("name,n", CASES)
-def test_fast_build_matches_oracle(name, n):
+@pytest.mark.parametrize("ctas", [3, 5])
+def test_fast_build_matches_oracle(name, n, ctas):
     w = synth.workload(name, n=n)
     nsteps = 3
-    ls = lsgb300.from_workload(w)
+    ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
     hist, done = ls.solve(nsteps)
     st = ls.stats()
     ref, nbs, iters, ost = _oracle(w, False, 0.0, nsteps)
@@ -87,6 +88,27 @@ def test_fast_build_matches_oracle(name, n):
         assert band.sum() > 0
         assert np.mean(e <= 1e-3) >= 0.98, (s, np.mean(e <= 1e-3), e.max())
     assert abs(st["nb_vertex_updates"] - ost["nb_vertex_updates"]) <= 0.005 * ost["nb_vertex_updates"]
+
+
+@pytest.mark.parametrize("name,n,update", [("c3", 14, None), ("c2", 9, None), ("c3", 18, "none")])
+def test_two_copies_per_thread_sweep_equals_one_copy_sweep(name, n, update):
+    # fim_ctas_per_sm 5 runs the tet sweep with two element copies per thread
+    # (state in shared memory); the solves, their listing and the per-vertex
+    # minimum are the same, so the results and the work counters are equal
+    w = synth.workload(name, n=n)
+    if update:
+        w["update"] = update
+    nsteps = 4
+    runs = []
+    for ctas in (3, 5):
+        ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
+        hist, done = ls.solve(nsteps)
+        runs.append((hist, done, ls.stats()))
+    (h3, d3, s3), (h5, d5, s5) = runs
+    assert d3 == d5 == nsteps
+    assert np.array_equal(h3, h5)
+    for key in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
+        assert s3[key] == s5[key], key
 
 
 @pytest.mark.parametrize("update", ["none", "curvature"])
