@@ -285,7 +285,10 @@ __device__ __forceinline__ R tet_solve(R TA, R TB, R TC, R ACAC, R ACBC, R ACCD,
 // The same tet update with predicated candidates instead of branches (fast
 // build): every quadratic's roots and candidate distances are evaluated and
 // the invalid ones masked, so the lanes of a warp stay converged through the
-// solve.  Valid candidates use the same expressions as tet_solve; CHK adds
+// solve.  A negative discriminant gives NaN roots, which fail every range
+// test, and a candidate whose distance is not a number is dropped by fminf,
+// so neither needs a guard.  Valid candidates use the same expressions as
+// tet_solve; CHK adds
 // the precision form's flags and cancellation-free roots (as tet_solve with
 // CHK, without its lower-bound skip, which the caller has applied).
 template <bool CHK = false>
@@ -303,16 +306,15 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   delta = q * q - 4.f * p * r;
   if (CHK && fmaxf(TB, TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
-    const bool ok = delta >= 0.f;
-    const float sq = sqrtf(fmaxf(delta, 0.f));
+    const float sq = sqrtf(delta);  // NaN when delta < 0: every root test fails
     float ra, rb;
     roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
       const float l2 = sgn ? rb : ra;
       const float l3 = 1.f - l2;
-      const float c = TB * l2 + TC * l3 + sqrtf(fmaxf((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD), 0.f));
-      if (ok && l2 >= 0.f && l2 <= 1.f) FaceTBC = fminf(FaceTBC, c);
+      const float c = TB * l2 + TC * l3 + sqrtf((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD));
+      if (l2 >= 0.f && l2 <= 1.f) FaceTBC = fminf(FaceTBC, c);
     }
   }
   FaceTBC = fminf(FaceTBC, fminf(TB + sqrtf((BCBC + BCCD) + (BCCD + CDCD)), TC + sqrtf(CDCD)));
@@ -327,8 +329,7 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   delta = q * q - 4.f * p * r;
   if (CHK && fmaxf(TA, TB) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
-    const bool ok = delta >= 0.f;
-    const float sq = sqrtf(fmaxf(delta, 0.f));
+    const float sq = sqrtf(delta);  // NaN when delta < 0: every root test fails
     float ra, rb;
     roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
@@ -336,10 +337,9 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
       const float l1 = sgn ? rb : ra;
       const float l2 = 1.f - l1;
       const float c = TA * l1 + TB * l2 +
-                      sqrtf(fmaxf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                                      (l1 * ACCD + l2 * BCCD + CDCD),
-                                  0.f));
-      if (ok && l1 >= 0.f && l1 <= 1.f) FaceTAB = fminf(FaceTAB, c);
+                      sqrtf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                            (l1 * ACCD + l2 * BCCD + CDCD));
+      if (l1 >= 0.f && l1 <= 1.f) FaceTAB = fminf(FaceTAB, c);
     }
   }
   FaceTAB = fminf(FaceTAB, fminf(TB + sqrtf((BCBC + BCCD) + (BCCD + CDCD)), TA + sqrtf((ACAC + ACCD) + (ACCD + CDCD))));
@@ -350,16 +350,15 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   delta = q * q - 4.f * p * r;
   if (CHK && fmaxf(TA, TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
-    const bool ok = delta >= 0.f;
-    const float sq = sqrtf(fmaxf(delta, 0.f));
+    const float sq = sqrtf(delta);  // NaN when delta < 0: every root test fails
     float ra, rb;
     roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
       const float l1 = sgn ? rb : ra;
       const float l3 = 1.f - l1;
-      const float c = TA * l1 + TC * l3 + sqrtf(fmaxf((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD), 0.f));
-      if (ok && l1 >= 0.f && l1 <= 1.f) FaceTAC = fminf(FaceTAC, c);
+      const float c = TA * l1 + TC * l3 + sqrtf((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD));
+      if (l1 >= 0.f && l1 <= 1.f) FaceTAC = fminf(FaceTAC, c);
     }
   }
   FaceTAC = fminf(FaceTAC, fminf(TA + sqrtf((ACAC + ACCD) + (ACCD + CDCD)), TC + sqrtf(CDCD)));
@@ -376,8 +375,7 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   delta = q * q - 4.f * p * r;
   if (CHK && fmaxf(fmaxf(TA, TB), TC) < LN && fabsf(delta) <= tau * (q * q + fabsf(4.f * p * r))) *ill = true;
   {
-    const bool ok = delta >= 0.f;
-    const float sq = sqrtf(fmaxf(delta, 0.f));
+    const float sq = sqrtf(delta);  // NaN when delta < 0: every root test fails
     float ra, rb;
     roots<float, CHK>(p, q, r, sq, ra, rb);
 #pragma unroll
@@ -386,10 +384,9 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
       const float l2 = (s * l1 + t) / (h + eps_h);
       const float l3 = 1.f - l1 - l2;
       const float c = TA * l1 + TB * l2 + TC * l3 +
-                      sqrtf(fmaxf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                                      (l1 * ACCD + l2 * BCCD + CDCD),
-                                  0.f));
-      if (ok && l1 >= 0.f && l1 <= 1.f && l2 >= 0.f && l2 <= 1.f && l3 >= 0.f && l3 <= 1.f) TD = fminf(TD, c);
+                      sqrtf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
+                            (l1 * ACCD + l2 * BCCD + CDCD));
+      if (l1 >= 0.f && l1 <= 1.f && l2 >= 0.f && l2 <= 1.f && l3 >= 0.f && l3 <= 1.f) TD = fminf(TD, c);
     }
   }
   return fminf(TD, fminf(FaceTBC, fminf(FaceTAB, FaceTAC)));
