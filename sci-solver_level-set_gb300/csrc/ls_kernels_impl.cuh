@@ -457,6 +457,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       hgt[1] = sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f));  // B over ACD
       hgt[2] = sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f));  // C over ABD
       hgt[3] = sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f));  // D over ABC
+#pragma unroll
+      for (int k = 0; k < 4; ++k) sH[k * MAXT + tid] = hgt[k];
     }
     // vertices of this copy whose value changed in the previous sweep (all
     // on the first): a solve whose three inputs are unchanged returns what
@@ -526,7 +528,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         if constexpr (PREC)
           r = tet_solve_pred<true>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum, sp.tau, &ill);
         else
-          r = tet_solve_pred<false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum);
+          r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, sH[k * MAXT + cc], sp.eps_h, sp.largenum);
         if (PREC && ill) {
           // discriminant cancelled: repeat in FP64 after this pass, densely
           sRep[atomicAdd(&s_rep, 1)] = code;
@@ -755,7 +757,9 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
         else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
         else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
-        const float r = tet_solve_pred<false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h, sp.largenum);
+        const float4 hv = sH[cc];
+        const float hD = k == 0 ? hv.x : k == 1 ? hv.y : k == 2 ? hv.z : hv.w;
+        const float r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, hD, sp.eps_h, sp.largenum);
         const float nw = fminf(own, r);
         const ushort4 cv = sC[cc];
         const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;

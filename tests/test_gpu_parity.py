@@ -113,8 +113,9 @@ def test_two_copies_per_thread_sweep_equals_one_copy_sweep(name, n, update):
 
 @pytest.mark.parametrize("update", ["none", "curvature"])
 def test_precision_form_meets_fp64_bar(update):
-    # the metric's accuracy bar, max |phi - phi_FP64| <= 1e-3 h, met by the
-    # precision form; plain FP32 keeps >= 99% of the band within it
+    # the metric's accuracy bar, max |phi - phi_FP64| <= 1e-3 h against the
+    # oracle run in FP64, met by the precision form (the reference's solver
+    # with FP64 repeats) and by the plain fast build (the planar-wave solver)
     w = synth.workload("c3", n=24)
     w["update"] = update
     nsteps = 3
@@ -127,8 +128,27 @@ def test_precision_form_meets_fp64_bar(update):
         e, _ = _band_err(hp[s], ref[s], w)
         assert e.max() <= 1e-3, (s, e.max())
         e, _ = _band_err(hf[s], ref[s], w)
-        assert np.mean(e <= 1e-3) >= 0.98, (s, np.mean(e <= 1e-3), e.max())
+        assert e.max() <= 1e-3, (s, e.max())
     assert prec.stats()["flagged_copies"] > 0
+
+
+@pytest.mark.parametrize("name,n,update,nsteps", [("c3", 20, "curvature", 4), ("c3", 28, "none", 2),
+                                                  ("c2", 16, "none", 2), ("c2", 12, "advect", 6)])
+def test_fast_build_meets_fp64_bar(name, n, update, nsteps):
+    # plain FP32 fast build against the oracle run in FP64 (every operation in
+    # double): the planar-wave tet solver has no cancelling discriminant, so
+    # the redistance stays at the FP64 result; the bar is 1e-3 h, the
+    # reference's FP32 solver misses it by up to ~1e-1 h on these inputs
+    w = synth.workload(name, n=n)
+    w["update"] = update
+    ref, _, _, _ = _oracle(w, False, 0.0, nsteps, precision=64)
+    ls = lsgb300.from_workload(w)
+    hist, done = ls.solve(nsteps)
+    assert done == nsteps
+    for s in range(1, nsteps + 1):
+        e, band = _band_err(hist[s], ref[s], w)
+        assert band.sum() > 0
+        assert e.max() <= 1e-3, (s, e.max())
 
 
 @pytest.mark.parametrize("staging", [False, True])
