@@ -440,8 +440,11 @@ def main():
     step_ms_prof = (ps["ms_sweep"] + ps["ms_check"] + ps["ms_schedule"] + ps["ms_seed"] + ps["ms_narrowband"]
                     + ps["ms_update"])
     kernel_ms = {k: ps["ms_" + k] / prof_steps for k in ("sweep", "check", "schedule", "seed", "narrowband", "update")}
+    # the sweep kernel the run used: two element copies per thread at the
+    # setting 5 (patches of up to 384 copies), one per thread otherwise
+    sweep_kernel = "k_fim_pair" if ls.get_params().fim_ctas_per_sm == 5 else "k_fim_compact"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profile_traffic(), "kernel": "k_fim_compact (FIM patch sweep launches)",
+                "traffic": profile_traffic(), "kernel": sweep_kernel + " (FIM patch sweep launches)",
                 "peak_source": peak_kind,
                 "share_of_step": (ps["ms_sweep"] / step_ms_prof) if step_ms_prof > 0 else None,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": sweep_ms}
