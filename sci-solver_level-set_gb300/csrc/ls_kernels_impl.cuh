@@ -644,6 +644,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   unsigned char* sF = reinterpret_cast<unsigned char*>(sItem + 4 * ncap);
   __shared__ unsigned s_min;
   __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
+  __shared__ int s_li;    // list entry of the next patch
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -660,8 +661,15 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  if (tid == 0) { s_n[0] = s_n[1] = 0; }
-  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+  // patches are taken from the list dynamically (one counter per launch
+  // kind), so that the CTAs that drew cheap patches take more of them
+  int* next = s.sched + (CHECK ? 1 : 0);
+  if (tid == 0) {
+    s_n[0] = s_n[1] = 0;
+    s_li = atomicAdd(next, 1);
+  }
+  __syncthreads();
+  for (int li = s_li; li < count;) {
     const int p = list[li];
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
@@ -825,6 +833,19 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       }
     }
     __syncthreads();
+    if (tid == 0) s_li = atomicAdd(next, 1);
+    __syncthreads();
+    li = s_li;
+  }
+  // the last CTA to finish resets this launch kind's counters: every CTA has
+  // drawn its last entry before it counts itself finished
+  if (tid == 0) {
+    __threadfence();
+    int* done = s.sched + (CHECK ? 3 : 2);
+    if (atomicAdd(done, 1) == (int)gridDim.x - 1) {
+      atomicExch(next, 0);
+      atomicExch(done, 0);
+    }
   }
 }
 

@@ -187,10 +187,12 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(dalloc(A, &s_.counts, 8), "alloc");
   LS_TRY(dalloc(A, &s_.stats, 8), "alloc");
   LS_TRY(dalloc(A, &s_.ctl, 4), "alloc");
+  LS_TRY(dalloc(A, &s_.sched, 4), "alloc");
   LS_TRY(dalloc(A, &d_tmp_, nv), "alloc");
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 8, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 8, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.ctl, 0, sizeof(int) * 4, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.sched, 0, sizeof(int) * 4, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.phi, 0, sizeof(float) * nv, stream_), "memset");
   LS_TRY(cudaMallocHost((void**)&h_counts_, sizeof(int) * 12), "pinned");
   LS_TRY(cudaMallocHost((void**)&h_stats_, sizeof(unsigned long long) * 8), "pinned");
