@@ -408,6 +408,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   __shared__ int s_rep;
   __shared__ unsigned s_min;
   __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
+  __shared__ int s_li;    // list entry of the next patch
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -424,9 +425,16 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  if (tid == 0) { s_n[0] = s_n[1] = 0; s_rep = 0; }
+  // patches are taken from the list dynamically, as in k_fim_pair
+  int* next = s.sched + (CHECK ? 1 : 0);
+  if (tid == 0) {
+    s_n[0] = s_n[1] = 0;
+    s_rep = 0;
+    s_li = atomicAdd(next, 1);
+  }
+  __syncthreads();
   int nflag = 0;
-  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+  for (int li = s_li; li < count;) {
     const int p = list[li];
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
@@ -607,6 +615,17 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       }
     }
     __syncthreads();
+    if (tid == 0) s_li = atomicAdd(next, 1);
+    __syncthreads();
+    li = s_li;
+  }
+  if (tid == 0) {
+    __threadfence();
+    int* done = s.sched + (CHECK ? 3 : 2);
+    if (atomicAdd(done, 1) == (int)gridDim.x - 1) {
+      atomicExch(next, 0);
+      atomicExch(done, 0);
+    }
   }
   if (PREC) {
     nflag = __reduce_add_sync(0xffffffffu, nflag);
