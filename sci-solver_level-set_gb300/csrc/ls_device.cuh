@@ -114,6 +114,11 @@ __device__ __forceinline__ PatchPar patch_par(const DevMesh& m, const StepParams
 
 enum { LS_FAR = 0, LS_ACTIVE = 1 };
 
+// Mark on an active-list entry: the patch was already visited by the
+// neighbour check that activated it (k_fim_pair); the sweep skips it and the
+// schedule masks the mark off.
+constexpr int kPrevisited = 1 << 30;
+
 template <typename R>
 __device__ __forceinline__ R rmin(R a, R b) { return fmin(a, b); }
 template <typename R>

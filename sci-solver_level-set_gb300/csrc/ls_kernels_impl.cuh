@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
   for (int li = blockIdx.x; li < count; li += gridDim.x) {
-    const int p = list[li];
+    const int p = list[li] & ~kPrevisited;  // re-visiting is harmless: same inputs, same results
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
     const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   __syncthreads();
   int nflag = 0;
   for (int li = s_li; li < count;) {
-    const int p = list[li];
+    const int p = list[li] & ~kPrevisited;  // re-visiting is harmless: same inputs, same results
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
     const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
@@ -633,6 +633,33 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   }
 }
 
+// One listed solve of k_fim_pair: solve k of copy cc from the copy values
+// at the sweep start; the result lowers the owned target's shared value or
+// becomes the copy's private ghost value.
+__device__ __forceinline__ void pair_solve(int code, const float4* sTc, const float4* sM, const float4* sH,
+                                           const ushort4* sC, float* sT, float4* sR, int nvp, const StepParams& sp) {
+  const int cc = code >> 2, k = code & 3;
+  const float4 tv = sTc[cc];
+  const float4 m0 = sM[3 * cc], m1 = sM[3 * cc + 1], m2 = sM[3 * cc + 2];
+  const float TA = tv.x, TB = tv.y, TC = tv.z, TD = tv.w;
+  const float ACAC = m0.x, ACBC = m0.y, ACCD = m0.z, BCBC = m0.w, BCCD = m1.x, CDCD = m1.y;
+  const float ADAD = m1.z, ADBD = m1.w, ADCD = m2.x, BDBD = m2.y, CDBD = m2.z;
+  // the permuted arguments of solve k (solve_copy's four calls)
+  float a0, a1, a2, g0, g1, g2, g3, g4, g5, own;
+  if (k == 3) { a0 = TA; a1 = TB; a2 = TC; g0 = ACAC; g1 = ACBC; g2 = ACCD; g3 = BCBC; g4 = BCCD; g5 = CDCD; own = TD; }
+  else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
+  else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
+  else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
+  const float4 hv = sH[cc];
+  const float hD = k == 0 ? hv.x : k == 1 ? hv.y : k == 2 ? hv.z : hv.w;
+  const float r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, hD, sp.eps_h, sp.largenum);
+  const float nw = fminf(own, r);
+  const ushort4 cv = sC[cc];
+  const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
+  if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(nw));
+  else reinterpret_cast<float*>(sR)[4 * cc + k] = nw;
+}
+
 // Fast-build FIM patch visit for tetrahedra, two element copies per thread.
 // The same sweep as k_fim_compact (listing with the lower bound, the
 // unchanged-input and unread-ghost skips; dense predicated solves; per-vertex
@@ -664,6 +691,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   __shared__ unsigned s_min;
   __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
   __shared__ int s_li;    // list entry of the next patch
+  __shared__ int s_ng;    // ghost-target solves listed when a check becomes a visit
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -689,13 +717,20 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   }
   __syncthreads();
   for (int li = s_li; li < count;) {
-    const int p = list[li];
+   const int entry = list[li];
+   // an entry marked as visited ahead was visited by the check that activated
+   // it, from the inputs this sweep would read: nothing is left to do
+   if (!(entry & kPrevisited)) {
+    const int p = entry;
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
     const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
     for (int i = tid; i < nvp + ngp; i += blockDim.x)
       sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
-    if (tid == 0) s_min = 0x7f800000u;
+    if (tid == 0) {
+      s_min = 0x7f800000u;
+      s_ng = 0;
+    }
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
@@ -722,16 +757,19 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
       }
     }
+    // a check that finds its patch unconverged turns into that patch's visit
+    int niter_p = niter;
+    bool visit = !CHECK;
     unsigned need[2] = {0u, 0u};
 #pragma unroll 1
-    for (int it = 0; it < niter; ++it) {
-      if (it == niter - 1) {
+    for (int it = 0; it < niter_p; ++it) {
+      if (it == niter_p - 1) {
         for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
         __syncthreads();
       }
       // list this thread's solves that can lower their target (the tests of
       // k_fim_compact)
-      const unsigned allow_ghost = (it == niter - 1) ? 0u : 0xFu;
+      const unsigned allow_ghost = (it == niter_p - 1) ? 0u : 0xFu;
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
@@ -770,30 +808,53 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       // the other parity's counter is idle until the next sweep's listing,
       // which starts after the barrier below
       if (tid == 0) s_n[(it & 1) ^ 1] = 0;
-      for (int i = tid; i < nitems; i += blockDim.x) {
-        const int code = sItem[i];
-        const int cc = code >> 2, k = code & 3;
-        const float4 tv = sTc[cc];
-        const float4 m0 = sM[3 * cc], m1 = sM[3 * cc + 1], m2 = sM[3 * cc + 2];
-        const float TA = tv.x, TB = tv.y, TC = tv.z, TD = tv.w;
-        const float ACAC = m0.x, ACBC = m0.y, ACCD = m0.z, BCBC = m0.w, BCCD = m1.x, CDCD = m1.y;
-        const float ADAD = m1.z, ADBD = m1.w, ADCD = m2.x, BDBD = m2.y, CDBD = m2.z;
-        // the permuted arguments of solve k (solve_copy's four calls)
-        float a0, a1, a2, g0, g1, g2, g3, g4, g5, own;
-        if (k == 3) { a0 = TA; a1 = TB; a2 = TC; g0 = ACAC; g1 = ACBC; g2 = ACCD; g3 = BCBC; g4 = BCCD; g5 = CDCD; own = TD; }
-        else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
-        else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
-        else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
-        const float4 hv = sH[cc];
-        const float hD = k == 0 ? hv.x : k == 1 ? hv.y : k == 2 ? hv.z : hv.w;
-        const float r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, hD, sp.eps_h, sp.largenum);
-        const float nw = fminf(own, r);
-        const ushort4 cv = sC[cc];
-        const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
-        if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(nw));
-        else reinterpret_cast<float*>(sR)[4 * cc + k] = nw;
-      }
+      for (int i = tid; i < nitems; i += blockDim.x) pair_solve(sItem[i], sTc, sM, sH, sC, sT, sR, nvp, sp);
       __syncthreads();
+      if (CHECK && !visit) {
+        // the check's verdict (as at the end of a check): does an owned
+        // vertex drop by tol or more?
+        int c0 = 1;
+        for (int i = tid; i < nvp; i += blockDim.x)
+          if (!s.seed[vs + i]) c0 &= (sOld[i] - sT[i] < sp.tol) ? 1 : 0;
+        if (!__syncthreads_and(c0) && sp.niter > 1) {
+          // activated: the patch's visit in the next FIM iteration would read
+          // the same DT (DT changes only in the copy-back after the sweeps), so
+          // it runs here and the next sweep skips the patch.  This sweep was
+          // its first sweep minus the ghost targets (the check's last-sweep
+          // rule): list and run those from the same sweep-start values.
+          visit = true;
+          niter_p = sp.niter;
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const int c = tid + j * blockDim.x;
+            if (c < nep) {
+              const float4 tv = sTc[c];
+              const float4 hv = sH[c];
+              const unsigned ghost = sF[c] >> 4;  // all four inputs count as changed
+              const float LN = sp.largenum;
+              const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
+              const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
+              unsigned nd = 0u;
+              if ((ghost & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
+              if ((ghost & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
+              if ((ghost & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
+              if ((ghost & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
+              need[j] |= nd;
+              const int n = __popc(nd);
+              if (n) {
+                int pos = nitems + atomicAdd(&s_ng, n);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                  if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
+              }
+            }
+          }
+          __syncthreads();
+          const int ng = s_ng;
+          for (int i = tid; i < ng; i += blockDim.x) pair_solve(sItem[nitems + i], sTc, sM, sH, sC, sT, sR, nvp, sp);
+          __syncthreads();
+        }
+      }
       // refresh this thread's copies: owned vertices from the per-vertex
       // minimum, ghost vertices from this sweep's own result where solved
 #pragma unroll
@@ -827,30 +888,34 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       const float nt = sT[i];
       float outv;
       if (!s.seed[v]) {
-        if (!CHECK) s.DT_out[v] = nt;
+        if (visit) s.DT_out[v] = nt;
         con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
         outv = nt;
       } else {
         outv = s.DT[v];
       }
-      if (!CHECK) atomicMin(&s_min, __float_as_uint(outv));
+      if (visit) atomicMin(&s_min, __float_as_uint(outv));
     }
     con = __syncthreads_and(con);
     if (tid == 0) {
-      if (!CHECK) {
+      if (visit) {
         atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
         s.bcon[p] = con;
         s.bmin[p] = __uint_as_float(s_min);
         s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
-      } else {
-        if (!con) {
+      }
+      if (CHECK) {
+        if (visit || !con) {
+          // activated: joins the next iteration's list (marked when visited
+          // here already)
           const int pos = atomicAdd(&s.counts[nxt], 1);
-          nlist[pos] = p;
+          nlist[pos] = visit ? (p | kPrevisited) : p;
         } else {
           s.blabel[p] = LS_FAR;
         }
       }
     }
+   }
     __syncthreads();
     if (tid == 0) s_li = atomicAdd(next, 1);
     __syncthreads();
@@ -877,7 +942,7 @@ __global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int w = warp_id_global(); w < count; w += nwarps) {
-    const int p = list[w];
+    const int p = list[w] & ~kPrevisited;
     const int vs = m.vert_off[p], ve = m.vert_off[p + 1];
     for (int v = vs + lane; v < ve; v += 32)
       if (!s.seed[v]) s.DT[v] = s.DT_out[v];

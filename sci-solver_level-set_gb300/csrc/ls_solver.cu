@@ -67,6 +67,8 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   cfg_ = cfg;
   K_ = cfg.bit_exact ? &kernels_exact() : &kernels_fast();
   if (L.lep > 1024) { status_ = 2; return "a patch has more than 1024 element copies"; }
+  // active-list entries carry the visited-ahead mark above the patch id
+  if (L.nparts >= kPrevisited) return "too many patches";
   LS_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
   {
     int dev = 0;
@@ -786,6 +788,7 @@ std::string Solver::active_patches(std::vector<int>& out) {
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   out.assign(h_counts_[0], 0);
   if (h_counts_[0] > 0) LS_TRY(cudaMemcpy(out.data(), s_.list0, sizeof(int) * h_counts_[0], cudaMemcpyDeviceToHost), "d2h");
+  for (int& p : out) p &= ~kPrevisited;
   return "";
 }
 
