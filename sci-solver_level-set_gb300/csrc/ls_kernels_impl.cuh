@@ -1067,23 +1067,41 @@ __device__ __forceinline__ void update_copy(const DevMesh& m, const StepParams& 
     const float a21 = x[1][0], a22 = x[1][1], a23 = x[1][2];
     const float a31 = x[2][0], a32 = x[2][1], a33 = x[2][2];
     const float a41 = x[3][0], a42 = x[3][1], a43 = x[3][2];
-    const float det =
-        a11 * a22 * a33 + a11 * a23 * a42 + a11 * a32 * a43 + a12 * a21 * a43 + a12 * a23 * a31 +
-        a12 * a33 * a41 + a13 * a21 * a32 + a13 * a22 * a41 + a13 * a31 * a42 + a21 * a33 * a42 +
-        a22 * a31 * a43 + a23 * a32 * a41 - a11 * a22 * a43 - a11 * a23 * a32 - a11 * a33 * a42 -
-        a12 * a21 * a33 - a12 * a23 * a41 - a12 * a31 * a43 - a13 * a21 * a42 - a13 * a22 * a31 -
-        a13 * a32 * a41 - a21 * a32 * a43 - a22 * a33 * a41 - a23 * a31 * a42;
-    const float b11 = a22 * a33 + a23 * a42 + a32 * a43 - a22 * a43 - a23 * a32 - a33 * a42;
-    const float b12 = a12 * a43 + a13 * a32 + a33 * a42 - a12 * a33 - a13 * a42 - a32 * a43;
-    const float b13 = a12 * a23 + a13 * a42 + a22 * a43 - a12 * a43 - a13 * a22 - a23 * a42;
+    float det, b11, b12, b13, b21, b22, b23, b31, b32, b33;
+    if (kLbSkip && !sp.ref_compat) {
+      // fast build: the fourth vertex is the origin (a41 = a42 = a43 = 0), so
+      // the same sums with their zero terms left out and the others in their
+      // order (equal values; only the sign of an exactly zero cofactor can
+      // differ, so the bit-exact build keeps the reference's full sums)
+      det = a11 * a22 * a33 + a12 * a23 * a31 + a13 * a21 * a32 - a11 * a23 * a32 - a12 * a21 * a33 -
+            a13 * a22 * a31;
+      b11 = a22 * a33 - a23 * a32;
+      b12 = a13 * a32 - a12 * a33;
+      b13 = a12 * a23 - a13 * a22;
+      b21 = a23 * a31 - a21 * a33;
+      b22 = a11 * a33 - a13 * a31;
+      b23 = a13 * a21 - a11 * a23;
+      b31 = a21 * a32 - a22 * a31;
+      b32 = a12 * a31 - a11 * a32;
+      b33 = a11 * a22 - a12 * a21;
+    } else {
+      det = a11 * a22 * a33 + a11 * a23 * a42 + a11 * a32 * a43 + a12 * a21 * a43 + a12 * a23 * a31 +
+            a12 * a33 * a41 + a13 * a21 * a32 + a13 * a22 * a41 + a13 * a31 * a42 + a21 * a33 * a42 +
+            a22 * a31 * a43 + a23 * a32 * a41 - a11 * a22 * a43 - a11 * a23 * a32 - a11 * a33 * a42 -
+            a12 * a21 * a33 - a12 * a23 * a41 - a12 * a31 * a43 - a13 * a21 * a42 - a13 * a22 * a31 -
+            a13 * a32 * a41 - a21 * a32 * a43 - a22 * a33 * a41 - a23 * a31 * a42;
+      b11 = a22 * a33 + a23 * a42 + a32 * a43 - a22 * a43 - a23 * a32 - a33 * a42;
+      b12 = a12 * a43 + a13 * a32 + a33 * a42 - a12 * a33 - a13 * a42 - a32 * a43;
+      b13 = a12 * a23 + a13 * a42 + a22 * a43 - a12 * a43 - a13 * a22 - a23 * a42;
+      b21 = a21 * a43 + a23 * a31 + a33 * a41 - a21 * a33 - a23 * a41 - a31 * a43;
+      b22 = a11 * a33 + a13 * a41 + a31 * a43 - a11 * a43 - a13 * a31 - a33 * a41;
+      b23 = a11 * a43 + a13 * a21 + a23 * a41 - a11 * a23 - a13 * a41 - a21 * a43;
+      b31 = a21 * a32 + a22 * a41 + a31 * a42 - a21 * a42 - a22 * a31 - a32 * a41;
+      b32 = a11 * a42 + a12 * a31 + a32 * a41 - a11 * a32 - a12 * a41 - a31 * a42;
+      b33 = a11 * a22 + a12 * a41 + a21 * a42 - a11 * a42 - a12 * a21 - a22 * a41;
+    }
     const float b14 = a12 * a33 + a13 * a22 + a23 * a32 - a12 * a23 - a13 * a32 - a22 * a33;
-    const float b21 = a21 * a43 + a23 * a31 + a33 * a41 - a21 * a33 - a23 * a41 - a31 * a43;
-    const float b22 = a11 * a33 + a13 * a41 + a31 * a43 - a11 * a43 - a13 * a31 - a33 * a41;
-    const float b23 = a11 * a43 + a13 * a21 + a23 * a41 - a11 * a23 - a13 * a41 - a21 * a43;
     const float b24 = a11 * a23 + a13 * a31 + a21 * a33 - a11 * a33 - a13 * a21 - a23 * a31;
-    const float b31 = a21 * a32 + a22 * a41 + a31 * a42 - a21 * a42 - a22 * a31 - a32 * a41;
-    const float b32 = a11 * a42 + a12 * a31 + a32 * a41 - a11 * a32 - a12 * a41 - a31 * a42;
-    const float b33 = a11 * a22 + a12 * a41 + a21 * a42 - a11 * a42 - a12 * a21 - a22 * a41;
     const float b34 = a11 * a32 + a12 * a21 + a22 * a31 - a11 * a22 - a12 * a31 - a21 * a32;
     float nN[4][3] = {{b11 / det, b21 / det, b31 / det},
                       {b12 / det, b22 / det, b32 / det},
