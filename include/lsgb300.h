@@ -121,7 +121,7 @@ typedef struct ls_stats {
   /* LS_PROFILE only: per-kernel device time (ms) and launches */
   double ms_sweep, ms_check, ms_schedule, ms_seed, ms_narrowband, ms_update;
   long long n_sweep, n_check, n_schedule, n_seed, n_narrowband, n_update;
-  long long sweep_slab_bytes;   /* algorithmic bytes read+written by sweeps */
+  long long sweep_slab_bytes;   /* algorithmic bytes read+written by the FIM patch kernel (visits and checks) */
   long long kernel_launches;    /* kernels launched (graph kernels included) */
   /* learned warm start (ls_set_learned) */
   long long warm_vertices;      /* vertices started from the network's prediction */

@@ -369,6 +369,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
         s.bmin[p] = __uint_as_float(s_min);
         s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
       } else {
+        // a check reads the visit's slab but writes no DT_out
+        atomicAdd(&s.stats[7], (unsigned long long)(__ldg(m.patch_bytes + p) - 4 * nvp));
         if (!con) {
           const int pos = atomicAdd(&s.counts[nxt], 1);
           nlist[pos] = p;
@@ -606,6 +608,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
         s.bmin[p] = __uint_as_float(s_min);
         s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
       } else {
+        // a check reads the visit's slab but writes no DT_out
+        atomicAdd(&s.stats[7], (unsigned long long)(__ldg(m.patch_bytes + p) - 4 * nvp));
         if (!con) {
           const int pos = atomicAdd(&s.counts[nxt], 1);
           nlist[pos] = p;
@@ -905,6 +909,8 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
       }
       if (CHECK) {
+        // a check that stayed a check read the visit's slab but wrote no DT_out
+        if (!visit) atomicAdd(&s.stats[7], (unsigned long long)(__ldg(m.patch_bytes + p) - 4 * nvp));
         if (visit || !con) {
           // activated: joins the next iteration's list (marked when visited
           // here already)
