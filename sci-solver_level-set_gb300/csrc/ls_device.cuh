@@ -70,9 +70,9 @@ struct DevState {
   unsigned long long* stats;  // [0] visits [1] checks [2] nb verts [3] nb patch verts [4] nb patches [5] fim iters [6] flagged copies solved [7] sweep slab bytes
   int* ctl;         // step control: [0] FIM loop bodies run this step, [1] iteration cap hit,
                     // [2] previous narrowband valid (seed search restricted to it)
-  int* sched;       // dynamic patch assignment of the sweep kernel: [0] next list entry of a
-                    // sweep, [1] of a check, [2] [3] CTAs finished; zero between launches (the
-                    // last CTA of a launch resets its pair)
+  int* sched;       // dynamic patch assignment of the sweep kernels: [0] next list entry of a
+                    // sweep, [1] of a check; zero between launches (the launch's last draw
+                    // resets it)
 };
 
 // Learned warm start / training-pair collection buffers (null when off).

@@ -383,6 +383,19 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
   }
 }
 
+// Patch assignment of the sweep kernels: CTA b takes list entry b first
+// (consecutive CTA ids sit on different SMs, so a short list spreads over the
+// whole GPU), then draws entries gridDim.x, gridDim.x + 1, ... from the launch
+// kind's counter, so that CTAs that drew cheap patches take more.  Only CTAs
+// that had a first entry draw, each until its first miss: the draws number
+// max(count - gridDim.x, 0) + min(count, gridDim.x), and the last of them
+// (value count - 1) resets the counter for the next launch of the kind.
+__device__ __forceinline__ int draw_patch(int* next, int count) {
+  const int v = atomicAdd(next, 1);
+  if (v == count - 1) atomicExch(next, 0);
+  return (int)gridDim.x + v;
+}
+
 // Fast-build FIM patch visit for tetrahedra with compacted solves.  Same
 // visit semantics as k_fim (Jacobi within an element, private ghost values,
 // per-vertex minimum, convergence on the last sweep), reorganised so that
@@ -427,12 +440,12 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  // patches are taken from the list dynamically, as in k_fim_pair
+  // first entry by CTA index, later ones drawn from a counter (draw_patch)
   int* next = s.sched + (CHECK ? 1 : 0);
   if (tid == 0) {
     s_n[0] = s_n[1] = 0;
     s_rep = 0;
-    s_li = atomicAdd(next, 1);
+    s_li = blockIdx.x;
   }
   __syncthreads();
   int nflag = 0;
@@ -619,17 +632,9 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       }
     }
     __syncthreads();
-    if (tid == 0) s_li = atomicAdd(next, 1);
+    if (tid == 0) s_li = draw_patch(next, count);
     __syncthreads();
     li = s_li;
-  }
-  if (tid == 0) {
-    __threadfence();
-    int* done = s.sched + (CHECK ? 3 : 2);
-    if (atomicAdd(done, 1) == (int)gridDim.x - 1) {
-      atomicExch(next, 0);
-      atomicExch(done, 0);
-    }
   }
   if (PREC) {
     nflag = __reduce_add_sync(0xffffffffu, nflag);
@@ -712,12 +717,16 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  // patches are taken from the list dynamically (one counter per launch
-  // kind), so that the CTAs that drew cheap patches take more of them
+  // first entry by CTA index, later ones drawn from a counter (draw_patch)
   int* next = s.sched + (CHECK ? 1 : 0);
+  // visits run by the checks that activate them only pay when the check
+  // launch is throughput bound (two patches or more per resident CTA): on
+  // fewer patches they add a visit's length to the iteration, while the next
+  // sweep launch still waits for the patches that stayed active
+  const bool early = CHECK && sp.niter > 1 && count >= 2 * (int)gridDim.x;
   if (tid == 0) {
     s_n[0] = s_n[1] = 0;
-    s_li = atomicAdd(next, 1);
+    s_li = blockIdx.x;
   }
   __syncthreads();
   for (int li = s_li; li < count;) {
@@ -820,7 +829,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         int c0 = 1;
         for (int i = tid; i < nvp; i += blockDim.x)
           if (!s.seed[vs + i]) c0 &= (sOld[i] - sT[i] < sp.tol) ? 1 : 0;
-        if (!__syncthreads_and(c0) && sp.niter > 1) {
+        if (!__syncthreads_and(c0) && early) {
           // activated: the patch's visit in the next FIM iteration would read
           // the same DT (DT changes only in the copy-back after the sweeps), so
           // it runs here and the next sweep skips the patch.  This sweep was
@@ -923,19 +932,9 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
     }
    }
     __syncthreads();
-    if (tid == 0) s_li = atomicAdd(next, 1);
+    if (tid == 0) s_li = draw_patch(next, count);
     __syncthreads();
     li = s_li;
-  }
-  // the last CTA to finish resets this launch kind's counters: every CTA has
-  // drawn its last entry before it counts itself finished
-  if (tid == 0) {
-    __threadfence();
-    int* done = s.sched + (CHECK ? 3 : 2);
-    if (atomicAdd(done, 1) == (int)gridDim.x - 1) {
-      atomicExch(next, 0);
-      atomicExch(done, 0);
-    }
   }
 }
 
