@@ -683,6 +683,11 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
 // connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k),
 // flags uchar [ncap] (changed vertices in bits 0-3, ghost vertices in bits
 // 4-7).
+// Patches: the list entry of the CTA's index first, later ones from
+// draw_patch.  On a check launch of at least two patches per CTA, a check
+// that finds its patch unconverged goes on to run that patch's visit (the
+// next iteration's visit would read the same DT) and marks the patch's entry
+// in the next list with kPrevisited; the next sweep skips marked entries.
 template <int MINB>
 __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
   const bool CHECK = check != 0;
