@@ -130,6 +130,8 @@ typedef struct ls_stats {
   long long moved_vertices;     /* warm vertices the FIM moved by more than 1e-3 h */
   long long learned_fallbacks;  /* steps redone as plain FIM after 16 support rounds */
   long long pairs_collected;    /* training pairs recorded (ls_learn_collect) */
+  long long early_visits;       /* patch visits run by the neighbour check that activated the patch
+                                   (fast build, tetrahedra; counted in patch_visits too) */
 } ls_stats;
 
 typedef struct ls_handle ls_handle;

@@ -117,6 +117,7 @@ void fill_stats(const lsgb::SolverStats& t, ls_stats* s) {
   s->moved_vertices = t.moved_vertices;
   s->learned_fallbacks = t.learned_fallbacks;
   s->pairs_collected = t.pairs_collected;
+  s->early_visits = t.early_visits;
 }
 
 // Solver configuration from a handle's parameters.

@@ -67,7 +67,7 @@ struct DevState {
   int* newlist;     // neighbour candidates of this iteration
   int* nblist;      // narrowband patches
   int* counts;      // [0] list0, [1] list1, [2] newlist, [3] nblist, [4] fim iters (step)
-  unsigned long long* stats;  // [0] visits [1] checks [2] nb verts [3] nb patch verts [4] nb patches [5] fim iters [6] flagged copies solved [7] sweep slab bytes
+  unsigned long long* stats;  // [0] visits [1] checks [2] nb verts [3] nb patch verts [4] nb patches [5] fim iters [6] flagged copies solved [7] FIM slab bytes [8] visits run by checks
   int* ctl;         // step control: [0] FIM loop bodies run this step, [1] iteration cap hit,
                     // [2] previous narrowband valid (seed search restricted to it)
   int* sched;       // dynamic patch assignment of the sweep kernels: [0] next list entry of a

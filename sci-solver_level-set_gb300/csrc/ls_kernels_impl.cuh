@@ -925,6 +925,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       if (CHECK) {
         // a check that stayed a check read the visit's slab but wrote no DT_out
         if (!visit) atomicAdd(&s.stats[7], (unsigned long long)(__ldg(m.patch_bytes + p) - 4 * nvp));
+        if (visit) atomicAdd(&s.stats[8], 1ull);
         if (visit || !con) {
           // activated: joins the next iteration's list (marked when visited
           // here already)

@@ -187,17 +187,17 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(dalloc(A, &s_.newlist, np), "alloc");
   LS_TRY(dalloc(A, &s_.nblist, np), "alloc");
   LS_TRY(dalloc(A, &s_.counts, 8), "alloc");
-  LS_TRY(dalloc(A, &s_.stats, 8), "alloc");
+  LS_TRY(dalloc(A, &s_.stats, 9), "alloc");
   LS_TRY(dalloc(A, &s_.ctl, 4), "alloc");
   LS_TRY(dalloc(A, &s_.sched, 4), "alloc");
   LS_TRY(dalloc(A, &d_tmp_, nv), "alloc");
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 8, stream_), "memset");
-  LS_TRY(cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 8, stream_), "memset");
+  LS_TRY(cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 9, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.ctl, 0, sizeof(int) * 4, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.sched, 0, sizeof(int) * 4, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.phi, 0, sizeof(float) * nv, stream_), "memset");
   LS_TRY(cudaMallocHost((void**)&h_counts_, sizeof(int) * 12), "pinned");
-  LS_TRY(cudaMallocHost((void**)&h_stats_, sizeof(unsigned long long) * 8), "pinned");
+  LS_TRY(cudaMallocHost((void**)&h_stats_, sizeof(unsigned long long) * 9), "pinned");
   LS_TRY(cudaMallocHost((void**)&h_stage_, sizeof(float) * nv), "pinned");
 
   // parameters (FIM quantities in the FIM frame)
@@ -615,7 +615,7 @@ std::string Solver::learned_step(bool* empty_nb) {
 }
 
 void Solver::pull_stats() {
-  if (cudaMemcpy(h_stats_, s_.stats, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) return;
+  if (cudaMemcpy(h_stats_, s_.stats, sizeof(unsigned long long) * 9, cudaMemcpyDeviceToHost) != cudaSuccess) return;
   st_.patch_visits = (long long)h_stats_[0];
   st_.check_visits = (long long)h_stats_[1];
   st_.nb_vertex_updates = (long long)h_stats_[2];
@@ -624,6 +624,7 @@ void Solver::pull_stats() {
   st_.fim_iters = (long long)h_stats_[5];
   st_.sweep_slab_bytes = (long long)h_stats_[7];
   st_.flagged_copies = (long long)h_stats_[6];
+  st_.early_visits = (long long)h_stats_[8];
   auto& pend = prof_pending();
   for (auto& pe : pend) {
     float ms = 0;
@@ -802,7 +803,7 @@ void Solver::stats(SolverStats& s) const { s = st_; }
 
 void Solver::reset_stats() {
   st_ = SolverStats();
-  cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 8, stream_);
+  cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 9, stream_);
   cudaStreamSynchronize(stream_);
 }
 

@@ -82,6 +82,7 @@ struct SolverStats {
   // learned warm start
   long long warm_vertices = 0, unsupported_resets = 0, support_rounds = 0, moved_vertices = 0;
   long long learned_fallbacks = 0, pairs_collected = 0;
+  long long early_visits = 0;
 };
 
 class Solver {

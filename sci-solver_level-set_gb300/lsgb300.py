@@ -52,6 +52,7 @@ class Stats(ctypes.Structure):
         ("warm_vertices", ctypes.c_longlong), ("unsupported_resets", ctypes.c_longlong),
         ("support_rounds", ctypes.c_longlong), ("moved_vertices", ctypes.c_longlong),
         ("learned_fallbacks", ctypes.c_longlong), ("pairs_collected", ctypes.c_longlong),
+        ("early_visits", ctypes.c_longlong),
     ]
 
     def as_dict(self):

@@ -111,6 +111,26 @@ def test_two_copies_per_thread_sweep_equals_one_copy_sweep(name, n, update):
         assert s3[key] == s5[key], key
 
 
+def test_visits_run_by_checks_change_nothing():
+    # on a mesh whose neighbour-check launches hold two or more patches per
+    # resident CTA, the two-copies-per-thread kernel runs the visits of the
+    # patches its checks activate in the same launch; the one-copy kernel
+    # visits them in the next iteration: same bits, same work counters
+    w = synth.workload("c3", n=96)
+    nsteps = 3
+    runs = {}
+    for ctas in (3, 5):
+        ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
+        ls.step(nsteps)
+        runs[ctas] = (ls.phi(), ls.stats())
+    (p3, s3), (p5, s5) = runs[3], runs[5]
+    assert s5["early_visits"] > 0 and s3["early_visits"] == 0
+    assert s5["early_visits"] < s5["patch_visits"]
+    assert np.array_equal(p3, p5)
+    for key in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
+        assert s3[key] == s5[key], key
+
+
 @pytest.mark.parametrize("update", ["none", "curvature"])
 def test_precision_form_meets_fp64_bar(update):
     # the metric's accuracy bar, max |phi - phi_FP64| <= 1e-3 h against the
