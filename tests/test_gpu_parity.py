@@ -61,6 +61,40 @@ def test_bitexact_build_equals_oracle(name, n, ref_compat, fp64):
         assert st[k] == ost[k], k
 
 
+def _repartition(w, n, kind, size):
+    w = dict(w)
+    if kind == "block":
+        w["npart"], w["nparts"] = synth.structured_partition(3, n + 1, size)
+    else:
+        w["npart"], w["nparts"] = lsgb300.partition_graph(3, w["elems"], len(w["xyz"]), size)
+    return w
+
+
+# graph partitions of 27 and 40 vertices and 4^3-vertex blocks: patches of up
+# to 382, 481 and 672 element copies, i.e. the two-copies-per-thread sweep and
+# the 512- and 1024-thread sweeps (one copy per thread), in both builds
+@pytest.mark.parametrize("kind,size", [("graph", 27), ("graph", 40), ("block", 4)])
+def test_large_patches_match_oracle(kind, size):
+    n, nsteps = 14, 3
+    w = _repartition(synth.workload("c3", n=n), n, kind, size)
+    ex = lsgb300.from_workload(w, bit_exact=True)
+    he, de = ex.solve(nsteps)
+    ref, nbs, iters, ost = _oracle(w, False, 0.0, nsteps)
+    assert de == ost["steps_run"] == nsteps
+    assert np.array_equal(he.view(np.uint32), ref.view(np.uint32))
+    st = ex.stats()
+    for k in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
+        assert st[k] == ost[k], k
+    fast = lsgb300.from_workload(w)
+    hf, df = fast.solve(nsteps)
+    ref64, _, _, _ = _oracle(w, False, 0.0, nsteps, precision=64)
+    assert df == nsteps
+    for s in range(1, nsteps + 1):
+        e, band = _band_err(hf[s], ref64[s], w)
+        assert band.sum() > 0
+        assert e.max() <= 1e-3, (s, e.max())
+
+
 @pytest.mark.parametrize("name,n", [("c2", 9), ("c3", 14)])
 @pytest.mark.parametrize("update", ["none", "advect", "curvature"])
 def test_bitexact_update_kinds(name, n, update):
