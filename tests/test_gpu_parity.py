@@ -108,14 +108,18 @@ def test_bitexact_update_kinds(name, n, update):
 
 
 @pytest.mark.parametrize("name,n", CASES)
-@pytest.mark.parametrize("ctas", [3, 5])
-def test_fast_build_matches_oracle(name, n, ctas):
+@pytest.mark.parametrize("ctas,ref_compat", [(3, False), (5, False), (5, True)])
+def test_fast_build_matches_oracle(name, n, ctas, ref_compat):
+    # ref_compat: the reference's absolute SMALLNUM at unit-cube scale, where
+    # even its FP32 and FP64 results lie up to ~0.5 h apart at a few vertices;
+    # the bar is the same share of band vertices within 1e-3 h of the FP32
+    # oracle
     w = synth.workload(name, n=n)
     nsteps = 3
-    ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
+    ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas, ref_compat=ref_compat)
     hist, done = ls.solve(nsteps)
     st = ls.stats()
-    ref, nbs, iters, ost = _oracle(w, False, 0.0, nsteps)
+    ref, nbs, iters, ost = _oracle(w, ref_compat, 0.0, nsteps)
     assert done == nsteps
     for s in range(1, nsteps + 1):
         e, band = _band_err(hist[s], ref[s], w)
