@@ -792,10 +792,12 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         need[j] = 0u;
-        if (c < nep) {
+        // a copy none of whose values changed in the previous sweep lists
+        // nothing: its flags are read first
+        const unsigned fl = c < nep ? sF[c] : 0u;
+        if (fl & 0xFu) {
           const float4 tv = sTc[c];
           const float4 hv = sH[c];
-          const unsigned fl = sF[c];
           const unsigned chg = fl & 0xFu, ghost = fl >> 4;
           const float LN = sp.largenum;
           const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
