@@ -1240,7 +1240,7 @@ __device__ __forceinline__ void update_copy(const DevMesh& m, const StepParams& 
 }
 
 template <int D1>
-__global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParams sp) {
+__device__ __forceinline__ void update_patches(const DevMesh& m, const DevState& s, const StepParams& sp) {
   extern __shared__ float smem[];
   const int slab = sp.lvp + sp.lgp;
   float* sPhi = smem;                // slab
@@ -1319,6 +1319,18 @@ __global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParam
     }
     __syncthreads();
   }
+}
+
+template <int D1>
+__global__ void __launch_bounds__(512) k_update(DevMesh m, DevState s, StepParams sp) {
+  update_patches<D1>(m, s, sp);
+}
+
+// tetrahedra with patches of up to 384 element copies: three CTAs per SM
+// (which caps the registers at 56 without spills; the 512-thread form keeps
+// two)
+__global__ void __launch_bounds__(384, 3) k_update_384(DevMesh m, DevState s, StepParams sp) {
+  update_patches<4>(m, s, sp);
 }
 
 // phi := phi_out on narrowband patches (CopyOutBack_levelset3d)
@@ -1624,7 +1636,8 @@ cudaError_t launch_narrowband(const DevMesh& m, const DevState& s, const StepPar
 
 cudaError_t launch_update(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
                           cudaStream_t st) {
-  if (m.dim == 3) k_update<4><<<L.upd_grid, L.upd_block, L.upd_smem, st>>>(m, s, sp);
+  if (m.dim == 3 && L.upd_block <= 384) k_update_384<<<L.upd_grid, L.upd_block, L.upd_smem, st>>>(m, s, sp);
+  else if (m.dim == 3) k_update<4><<<L.upd_grid, L.upd_block, L.upd_smem, st>>>(m, s, sp);
   else k_update<3><<<L.upd_grid, L.upd_block, L.upd_smem, st>>>(m, s, sp);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -1717,14 +1730,16 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   L.upd_block = L.fim_block > 512 ? 512 : L.fim_block;
   const int slab = sp.lvp + sp.lgp;
   L.upd_smem = (int)sizeof(float) * (slab * (m.dim == 3 ? 4 : 1) + sp.lep * 16);
-  if (L.upd_smem > 48 * 1024) {
-    if (m.dim == 3) e = cudaFuncSetAttribute(k_update<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, L.upd_smem);
-    else e = cudaFuncSetAttribute(k_update<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, L.upd_smem);
-    if (e != cudaSuccess) return e;
+  {
+    const void* fn = m.dim == 3 ? (L.upd_block <= 384 ? (const void*)k_update_384 : (const void*)k_update<4>)
+                                : (const void*)k_update<3>;
+    if (L.upd_smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, L.upd_smem);
+      if (e != cudaSuccess) return e;
+    }
+    occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, L.upd_block, L.upd_smem);
   }
-  occ = 0;
-  if (m.dim == 3) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update<4>, L.upd_block, L.upd_smem);
-  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_update<3>, L.upd_block, L.upd_smem);
   if (e != cudaSuccess) return e;
   if (occ < 1) occ = 1;
   L.upd_grid = L.sms * occ;
