@@ -7,15 +7,24 @@
 //   k_reset        DT := LARGENUM, seed := 0, sign := (phi >= 0)     (whole mesh)
 //   k_seed         seed points and the first active patch list        (K9)
 //   FIM iterations, each:
-//     k_fim<SWEEP> NITER sweeps on every active patch, fused per-patch
+//     sweep        NITER sweeps on every active patch, fused per-patch
 //                  convergence AND and min (K11 + K13)
 //     k_schedule   copy-back, unconverged patches to the next list,
 //                  neighbours of converged patches with min < w to the
 //                  candidate list (the host loop of redistance3d.cu:139-181)
-//     k_fim<CHECK> one-sweep probe of the candidates; unconverged ones join
+//     check        one-sweep probe of the candidates; unconverged ones join
 //                  the next list (K12 + K13 + redistance3d.cu:188-222)
+//     The sweep and the check are one kernel with a runtime flag: k_fim
+//     (bit-exact build and triangles: one element copy per thread, the
+//     reference's solves in its order), k_fim_compact (fast build,
+//     tetrahedra: the solves that can lower a value listed and run densely,
+//     one copy per thread) and k_fim_pair (the same with two copies per
+//     thread, the default for patches of up to 384 copies; its checks also
+//     run the visits of the patches they activate on long check lists).
 //   k_narrowband   patch narrowband, phi := sign * DT, vertex-update count (K14 + K10b)
 //   k_update       advection (K16) or mean-curvature update on narrowband patches
+//                  (k_update_384: the same for patches of up to 384 copies,
+//                  three CTAs per SM)
 //   k_copy_phi     phi := phi_out on narrowband patches (K15)
 //   k_unpermute    phi in the caller's vertex order (K18)
 //
