@@ -744,210 +744,210 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   }
   __syncthreads();
   for (int li = s_li; li < count;) {
-   const int entry = list[li];
-   // an entry marked as visited ahead was visited by the check that activated
-   // it, from the inputs this sweep would read: nothing is left to do
-   if (!(entry & kPrevisited)) {
-    const int p = entry;
-    const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
-    const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
-    const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
-    for (int i = tid; i < nvp + ngp; i += blockDim.x)
-      sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
-    if (tid == 0) {
-      s_min = 0x7f800000u;
-      s_ng = 0;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int c = tid + j * blockDim.x;
-      if (c < nep) {
-        const ushort4 cv = m.conn[es + c];
-        sC[c] = cv;
-        sTc[c] = make_float4(sT[cv.x], sT[cv.y], sT[cv.z], sT[cv.w]);
-        float Mt[11];
-        copy_metric<4>(m, (long long)es + c, Mt);
-        sM[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
-        sM[3 * c + 1] = make_float4(Mt[4], Mt[5], Mt[6], Mt[7]);
-        sM[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], 0.f);
-        const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
-        const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
-        const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
-                           ACCD * (ACBC * BCCD - BCBC * ACCD);
-        sH[c] = make_float4(sqrtf(fmaxf(det3 / (BCBC * CDCD - BCCD * BCCD), 0.f)),   // A over BCD
-                            sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f)),   // B over ACD
-                            sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f)),   // C over ABD
-                            sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f)));  // D over ABC
-        const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
-                               (cv.w >= nvp ? 8u : 0u);
-        sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
-      }
-    }
-    // a check that finds its patch unconverged turns into that patch's visit
-    int niter_p = niter;
-    bool visit = !CHECK;
-    unsigned need[2] = {0u, 0u};
-#pragma unroll 1
-    for (int it = 0; it < niter_p; ++it) {
-      if (it == niter_p - 1) {
-        for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
-        __syncthreads();
-      }
-      // list this thread's solves that can lower their target (the tests of
-      // k_fim_compact)
-      const unsigned allow_ghost = (it == niter_p - 1) ? 0u : 0xFu;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int c = tid + j * blockDim.x;
-        need[j] = 0u;
-        // a copy none of whose values changed in the previous sweep lists
-        // nothing: its flags are read first
-        const unsigned fl = c < nep ? sF[c] : 0u;
-        if (fl & 0xFu) {
-          const float4 tv = sTc[c];
-          const float4 hv = sH[c];
-          const unsigned chg = fl & 0xFu, ghost = fl >> 4;
-          const float LN = sp.largenum;
-          const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
-          const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
-          unsigned cand = 0u;
-          if (chg & 0xEu) cand |= 1u;
-          if (chg & 0xDu) cand |= 2u;
-          if (chg & 0xBu) cand |= 4u;
-          if (chg & 0x7u) cand |= 8u;
-          cand &= (~ghost | allow_ghost) & 0xFu;
-          unsigned nd = 0u;
-          if ((cand & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
-          if ((cand & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
-          if ((cand & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
-          if ((cand & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
-          need[j] = nd;
-          const int n = __popc(nd);
-          if (n) {
-            int pos = atomicAdd(&s_n[it & 1], n);
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-              if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
-          }
-        }
+    const int entry = list[li];
+    // an entry marked as visited ahead was visited by the check that activated
+    // it, from the inputs this sweep would read: nothing is left to do
+    if (!(entry & kPrevisited)) {
+      const int p = entry;
+      const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
+      const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
+      const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+      for (int i = tid; i < nvp + ngp; i += blockDim.x)
+        sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
+      if (tid == 0) {
+        s_min = 0x7f800000u;
+        s_ng = 0;
       }
       __syncthreads();
-      const int nitems = s_n[it & 1];
-      // the other parity's counter is idle until the next sweep's listing,
-      // which starts after the barrier below
-      if (tid == 0) s_n[(it & 1) ^ 1] = 0;
-      for (int i = tid; i < nitems; i += blockDim.x) pair_solve(sItem[i], sTc, sM, sH, sC, sT, sR, nvp, sp);
-      __syncthreads();
-      if (CHECK && !visit) {
-        // the check's verdict (as at the end of a check): does an owned
-        // vertex drop by tol or more?
-        int c0 = 1;
-        for (int i = tid; i < nvp; i += blockDim.x)
-          if (!s.seed[vs + i]) c0 &= (sOld[i] - sT[i] < sp.tol) ? 1 : 0;
-        if (!__syncthreads_and(c0) && early) {
-          // activated: the patch's visit in the next FIM iteration would read
-          // the same DT (DT changes only in the copy-back after the sweeps), so
-          // it runs here and the next sweep skips the patch.  This sweep was
-          // its first sweep minus the ghost targets (the check's last-sweep
-          // rule): list and run those from the same sweep-start values.
-          visit = true;
-          niter_p = sp.niter;
-#pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            const int c = tid + j * blockDim.x;
-            if (c < nep) {
-              const float4 tv = sTc[c];
-              const float4 hv = sH[c];
-              const unsigned ghost = sF[c] >> 4;  // all four inputs count as changed
-              const float LN = sp.largenum;
-              const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
-              const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
-              unsigned nd = 0u;
-              if ((ghost & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
-              if ((ghost & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
-              if ((ghost & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
-              if ((ghost & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
-              need[j] |= nd;
-              const int n = __popc(nd);
-              if (n) {
-                int pos = nitems + atomicAdd(&s_ng, n);
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                  if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
-              }
-            }
-          }
-          __syncthreads();
-          const int ng = s_ng;
-          for (int i = tid; i < ng; i += blockDim.x) pair_solve(sItem[nitems + i], sTc, sM, sH, sC, sT, sR, nvp, sp);
-          __syncthreads();
-        }
-      }
-      // refresh this thread's copies: owned vertices from the per-vertex
-      // minimum, ghost vertices from this sweep's own result where solved
-#pragma unroll
+  #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         if (c < nep) {
-          const float4 tv = sTc[c];
-          const float4 rv = sR[c];
-          const ushort4 cv = sC[c];
-          const unsigned nd = need[j];
-          float4 nv;
-          nv.x = cv.x < nvp ? sT[cv.x] : ((nd & 1u) ? rv.x : tv.x);
-          nv.y = cv.y < nvp ? sT[cv.y] : ((nd & 2u) ? rv.y : tv.y);
-          nv.z = cv.z < nvp ? sT[cv.z] : ((nd & 4u) ? rv.z : tv.z);
-          nv.w = cv.w < nvp ? sT[cv.w] : ((nd & 8u) ? rv.w : tv.w);
-          const unsigned chg = (nv.x != tv.x ? 1u : 0u) | (nv.y != tv.y ? 2u : 0u) | (nv.z != tv.z ? 4u : 0u) |
-                               (nv.w != tv.w ? 8u : 0u);
-          sTc[c] = nv;
-          sF[c] = (unsigned char)((sF[c] & 0xF0u) | chg);
+          const ushort4 cv = m.conn[es + c];
+          sC[c] = cv;
+          sTc[c] = make_float4(sT[cv.x], sT[cv.y], sT[cv.z], sT[cv.w]);
+          float Mt[11];
+          copy_metric<4>(m, (long long)es + c, Mt);
+          sM[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
+          sM[3 * c + 1] = make_float4(Mt[4], Mt[5], Mt[6], Mt[7]);
+          sM[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], 0.f);
+          const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
+          const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
+          const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
+                             ACCD * (ACBC * BCCD - BCBC * ACCD);
+          sH[c] = make_float4(sqrtf(fmaxf(det3 / (BCBC * CDCD - BCCD * BCCD), 0.f)),   // A over BCD
+                              sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f)),   // B over ACD
+                              sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f)),   // C over ABD
+                              sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f)));  // D over ABC
+          const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
+                                 (cv.w >= nvp ? 8u : 0u);
+          sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
         }
       }
-      // no barrier here: every thread refreshes only its own copies, and the
-      // next sweep's solves read them after the barrier that follows its
-      // listing
-    }
-    __syncthreads();
-    if (tid == 0) s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
-    int con = 1;
-    for (int i = tid; i < nvp; i += blockDim.x) {
-      const int v = vs + i;
-      const float nt = sT[i];
-      float outv;
-      if (!s.seed[v]) {
-        if (visit) s.DT_out[v] = nt;
-        con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
-        outv = nt;
-      } else {
-        outv = s.DT[v];
+      // a check that finds its patch unconverged turns into that patch's visit
+      int niter_p = niter;
+      bool visit = !CHECK;
+      unsigned need[2] = {0u, 0u};
+  #pragma unroll 1
+      for (int it = 0; it < niter_p; ++it) {
+        if (it == niter_p - 1) {
+          for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
+          __syncthreads();
+        }
+        // list this thread's solves that can lower their target (the tests of
+        // k_fim_compact)
+        const unsigned allow_ghost = (it == niter_p - 1) ? 0u : 0xFu;
+  #pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int c = tid + j * blockDim.x;
+          need[j] = 0u;
+          // a copy none of whose values changed in the previous sweep lists
+          // nothing: its flags are read first
+          const unsigned fl = c < nep ? sF[c] : 0u;
+          if (fl & 0xFu) {
+            const float4 tv = sTc[c];
+            const float4 hv = sH[c];
+            const unsigned chg = fl & 0xFu, ghost = fl >> 4;
+            const float LN = sp.largenum;
+            const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
+            const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
+            unsigned cand = 0u;
+            if (chg & 0xEu) cand |= 1u;
+            if (chg & 0xDu) cand |= 2u;
+            if (chg & 0xBu) cand |= 4u;
+            if (chg & 0x7u) cand |= 8u;
+            cand &= (~ghost | allow_ghost) & 0xFu;
+            unsigned nd = 0u;
+            if ((cand & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
+            if ((cand & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
+            if ((cand & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
+            if ((cand & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
+            need[j] = nd;
+            const int n = __popc(nd);
+            if (n) {
+              int pos = atomicAdd(&s_n[it & 1], n);
+  #pragma unroll
+              for (int k = 0; k < 4; ++k)
+                if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
+            }
+          }
+        }
+        __syncthreads();
+        const int nitems = s_n[it & 1];
+        // the other parity's counter is idle until the next sweep's listing,
+        // which starts after the barrier below
+        if (tid == 0) s_n[(it & 1) ^ 1] = 0;
+        for (int i = tid; i < nitems; i += blockDim.x) pair_solve(sItem[i], sTc, sM, sH, sC, sT, sR, nvp, sp);
+        __syncthreads();
+        if (CHECK && !visit) {
+          // the check's verdict (as at the end of a check): does an owned
+          // vertex drop by tol or more?
+          int c0 = 1;
+          for (int i = tid; i < nvp; i += blockDim.x)
+            if (!s.seed[vs + i]) c0 &= (sOld[i] - sT[i] < sp.tol) ? 1 : 0;
+          if (!__syncthreads_and(c0) && early) {
+            // activated: the patch's visit in the next FIM iteration would read
+            // the same DT (DT changes only in the copy-back after the sweeps), so
+            // it runs here and the next sweep skips the patch.  This sweep was
+            // its first sweep minus the ghost targets (the check's last-sweep
+            // rule): list and run those from the same sweep-start values.
+            visit = true;
+            niter_p = sp.niter;
+  #pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int c = tid + j * blockDim.x;
+              if (c < nep) {
+                const float4 tv = sTc[c];
+                const float4 hv = sH[c];
+                const unsigned ghost = sF[c] >> 4;  // all four inputs count as changed
+                const float LN = sp.largenum;
+                const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
+                const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
+                unsigned nd = 0u;
+                if ((ghost & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
+                if ((ghost & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
+                if ((ghost & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
+                if ((ghost & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
+                need[j] |= nd;
+                const int n = __popc(nd);
+                if (n) {
+                  int pos = nitems + atomicAdd(&s_ng, n);
+  #pragma unroll
+                  for (int k = 0; k < 4; ++k)
+                    if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
+                }
+              }
+            }
+            __syncthreads();
+            const int ng = s_ng;
+            for (int i = tid; i < ng; i += blockDim.x) pair_solve(sItem[nitems + i], sTc, sM, sH, sC, sT, sR, nvp, sp);
+            __syncthreads();
+          }
+        }
+        // refresh this thread's copies: owned vertices from the per-vertex
+        // minimum, ghost vertices from this sweep's own result where solved
+  #pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int c = tid + j * blockDim.x;
+          if (c < nep) {
+            const float4 tv = sTc[c];
+            const float4 rv = sR[c];
+            const ushort4 cv = sC[c];
+            const unsigned nd = need[j];
+            float4 nv;
+            nv.x = cv.x < nvp ? sT[cv.x] : ((nd & 1u) ? rv.x : tv.x);
+            nv.y = cv.y < nvp ? sT[cv.y] : ((nd & 2u) ? rv.y : tv.y);
+            nv.z = cv.z < nvp ? sT[cv.z] : ((nd & 4u) ? rv.z : tv.z);
+            nv.w = cv.w < nvp ? sT[cv.w] : ((nd & 8u) ? rv.w : tv.w);
+            const unsigned chg = (nv.x != tv.x ? 1u : 0u) | (nv.y != tv.y ? 2u : 0u) | (nv.z != tv.z ? 4u : 0u) |
+                                 (nv.w != tv.w ? 8u : 0u);
+            sTc[c] = nv;
+            sF[c] = (unsigned char)((sF[c] & 0xF0u) | chg);
+          }
+        }
+        // no barrier here: every thread refreshes only its own copies, and the
+        // next sweep's solves read them after the barrier that follows its
+        // listing
       }
-      if (visit) atomicMin(&s_min, __float_as_uint(outv));
-    }
-    con = __syncthreads_and(con);
-    if (tid == 0) {
-      if (visit) {
-        atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
-        s.bcon[p] = con;
-        s.bmin[p] = __uint_as_float(s_min);
-        s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
-      }
-      if (CHECK) {
-        // a check that stayed a check read the visit's slab but wrote no DT_out
-        if (!visit) atomicAdd(&s.stats[7], (unsigned long long)(__ldg(m.patch_bytes + p) - 4 * nvp));
-        if (visit) atomicAdd(&s.stats[8], 1ull);
-        if (visit || !con) {
-          // activated: joins the next iteration's list (marked when visited
-          // here already)
-          const int pos = atomicAdd(&s.counts[nxt], 1);
-          nlist[pos] = visit ? (p | kPrevisited) : p;
+      __syncthreads();
+      if (tid == 0) s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
+      int con = 1;
+      for (int i = tid; i < nvp; i += blockDim.x) {
+        const int v = vs + i;
+        const float nt = sT[i];
+        float outv;
+        if (!s.seed[v]) {
+          if (visit) s.DT_out[v] = nt;
+          con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
+          outv = nt;
         } else {
-          s.blabel[p] = LS_FAR;
+          outv = s.DT[v];
+        }
+        if (visit) atomicMin(&s_min, __float_as_uint(outv));
+      }
+      con = __syncthreads_and(con);
+      if (tid == 0) {
+        if (visit) {
+          atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
+          s.bcon[p] = con;
+          s.bmin[p] = __uint_as_float(s_min);
+          s.blabel[p] = con ? LS_FAR : LS_ACTIVE;
+        }
+        if (CHECK) {
+          // a check that stayed a check read the visit's slab but wrote no DT_out
+          if (!visit) atomicAdd(&s.stats[7], (unsigned long long)(__ldg(m.patch_bytes + p) - 4 * nvp));
+          if (visit) atomicAdd(&s.stats[8], 1ull);
+          if (visit || !con) {
+            // activated: joins the next iteration's list (marked when visited
+            // here already)
+            const int pos = atomicAdd(&s.counts[nxt], 1);
+            nlist[pos] = visit ? (p | kPrevisited) : p;
+          } else {
+            s.blabel[p] = LS_FAR;
+          }
         }
       }
     }
-   }
     __syncthreads();
     if (tid == 0) s_li = draw_patch(next, count);
     __syncthreads();
