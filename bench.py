@@ -113,19 +113,25 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the FIM sweep kernel from the committed ncu
-    summary (profiles/k_fim_sweep_c3.md), or None."""
+def profile_value(key):
+    """A figure of the committed ncu summary of the FIM kernel
+    (profiles/k_fim_sweep_c3.md, lines "key: value"), or None."""
     path = os.path.join(ROOT, "profiles", "k_fim_sweep_c3.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the FIM kernel from the committed ncu summary,
+    or None."""
+    return profile_value("traffic_bytes_per_launch")
 
 
 def oracle_rate(w, nsteps, warm, threads, precision=32):
@@ -450,7 +456,12 @@ def main():
                 "traffic": profile_traffic(), "kernel": sweep_kernel + " (FIM patch sweep and check launches)",
                 "peak_source": peak_kind,
                 "share_of_step": ((ps["ms_sweep"] + ps["ms_check"]) / step_ms_prof) if step_ms_prof > 0 else None,
-                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": sweep_ms}
+                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": sweep_ms,
+                # the FIM kernel is bound by instruction issue of the local
+                # solvers, not by HBM: issue slots active from the committed
+                # ncu capture of its sweep and check launches
+                "limiter": "SM instruction issue (FP32/ALU/MUFU of the local solvers); DRAM at 3-6 % of peak",
+                "issue_slots_active": profile_value("issue_slots_active")}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
