@@ -13,8 +13,8 @@ Metric: narrowband vertex-updates per second, one update = one vertex with
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 With --gpus N > 1 (launched by torch.distributed.run) every rank runs an
-independent replica of the workload (the time step does not shard; see
-the design doc); the timed region is bracketed by a barrier and the maximum time
+independent replica of the workload (the time step does not shard: the
+wavefront couples neighbouring patches in every FIM iteration); the timed region is bracketed by a barrier and the maximum time
 over ranks is reported.
 """
 import argparse
