@@ -823,12 +823,19 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
             if ((cand & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
             if ((cand & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
             need[j] = nd;
-            const int n = __popc(nd);
-            if (n) {
-              int pos = atomicAdd(&s_n[it & 1], n);
+          }
+        }
+        {
+          // list positions: one shared atomic per thread for both copies
+          const int nt = __popc(need[0]) + __popc(need[1]);
+          if (nt) {
+            int pos = atomicAdd(&s_n[it & 1], nt);
+  #pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int c = tid + j * blockDim.x;
   #pragma unroll
               for (int k = 0; k < 4; ++k)
-                if (nd & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
+                if (need[j] & (1u << k)) sItem[pos++] = (unsigned short)((c << 2) | k);
             }
           }
         }
@@ -910,7 +917,15 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         // listing
       }
       __syncthreads();
-      if (tid == 0) s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
+      // the next list entry is drawn here (draw_patch in two parts), its
+      // atomic in flight during the copy-out below; s_li was read by every
+      // thread before the barrier above, and is read again after the one
+      // below
+      int drawn = 0;
+      if (tid == 0) {
+        s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
+        drawn = atomicAdd(next, 1);
+      }
       int con = 1;
       for (int i = tid; i < nvp; i += blockDim.x) {
         const int v = vs + i;
@@ -925,7 +940,12 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         }
         if (visit) atomicMin(&s_min, __float_as_uint(outv));
       }
+      if (tid == 0) {
+        if (drawn == count - 1) atomicExch(next, 0);
+        s_li = (int)gridDim.x + drawn;
+      }
       con = __syncthreads_and(con);
+      li = s_li;
       if (tid == 0) {
         if (visit) {
           atomicAdd(&s.stats[7], (unsigned long long)__ldg(m.patch_bytes + p));
@@ -947,11 +967,12 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
           }
         }
       }
+    } else {
+      __syncthreads();
+      if (tid == 0) s_li = draw_patch(next, count);
+      __syncthreads();
+      li = s_li;
     }
-    __syncthreads();
-    if (tid == 0) s_li = draw_patch(next, count);
-    __syncthreads();
-    li = s_li;
   }
 }
 
