@@ -47,6 +47,10 @@ Solver::~Solver() {
   if (h_stage_) cudaFreeHost(h_stage_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
+  for (auto& pe : prof_) {
+    cudaEventDestroy(pe.a);
+    cudaEventDestroy(pe.b);
+  }
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -334,19 +338,6 @@ std::string Solver::build_graph() {
   return "";
 }
 
-// Profiling helper: event pairs around launches when cfg_.profile is set.
-namespace {
-struct ProfEvent {
-  cudaEvent_t a, b;
-  int kind;
-};
-}  // namespace
-
-static std::vector<ProfEvent>& prof_pending() {
-  static thread_local std::vector<ProfEvent> v;
-  return v;
-}
-
 std::string Solver::fim_loop(const StepParams& sp) {
   long long launched = 0;
   auto prof = [&](int kind, auto&& fn) -> cudaError_t {
@@ -358,7 +349,7 @@ std::string Solver::fim_loop(const StepParams& sp) {
     cudaEventRecord(pe.a, stream_);
     cudaError_t e = fn();
     cudaEventRecord(pe.b, stream_);
-    prof_pending().push_back(pe);
+    prof_.push_back(pe);
     return e;
   };
   while (true) {
@@ -392,7 +383,7 @@ std::string Solver::one_step(bool* empty_nb) {
     cudaEventRecord(pe.a, stream_);
     cudaError_t e = fn();
     cudaEventRecord(pe.b, stream_);
-    prof_pending().push_back(pe);
+    prof_.push_back(pe);
     return e;
   };
   if (net_ || collect_) return learned_step(empty_nb);
@@ -614,8 +605,15 @@ std::string Solver::learned_step(bool* empty_nb) {
   return "";
 }
 
+// The work counters and the profiled launch times are read from the device
+// when a caller asks for them (stats), not after every step: a step through
+// host buffers then ends with its own result copy and no second round trip.
 void Solver::pull_stats() {
-  if (cudaMemcpy(h_stats_, s_.stats, sizeof(unsigned long long) * 9, cudaMemcpyDeviceToHost) != cudaSuccess) return;
+  if (cudaMemcpyAsync(h_stats_, s_.stats, sizeof(unsigned long long) * 9, cudaMemcpyDeviceToHost, stream_) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(stream_) != cudaSuccess)
+    return;
+  stats_stale_ = false;
   st_.patch_visits = (long long)h_stats_[0];
   st_.check_visits = (long long)h_stats_[1];
   st_.nb_vertex_updates = (long long)h_stats_[2];
@@ -625,7 +623,7 @@ void Solver::pull_stats() {
   st_.sweep_slab_bytes = (long long)h_stats_[7];
   st_.flagged_copies = (long long)h_stats_[6];
   st_.early_visits = (long long)h_stats_[8];
-  auto& pend = prof_pending();
+  auto& pend = prof_;
   for (auto& pe : pend) {
     float ms = 0;
     cudaEventElapsedTime(&ms, pe.a, pe.b);
@@ -672,7 +670,7 @@ std::string Solver::run(int nsteps, float* history, int* steps_done) {
   st_.ms_total += ms;
   st_.steps_run += done;
   if (steps_done) *steps_done = done;
-  pull_stats();
+  stats_stale_ = true;
   return "";
 }
 
@@ -703,7 +701,7 @@ std::string Solver::step_host(const float* phi_in, float* phi_out) {
     std::memcpy(phi_out, h_stage_, sizeof(float) * nv);
   }
   if (!empty) st_.steps_run++;
-  pull_stats();
+  stats_stale_ = true;
   return "";
 }
 
@@ -751,7 +749,7 @@ std::string Solver::eikonal(const int* seeds, const float* values, int nseeds, f
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   for (int v = 0; v < nv; ++v) out[L.vert_permute[v]] = (dt[v] >= LN) ? LN : dt[v] * sp_.scale;
   have_nb_ = false;  // the step state was overwritten
-  pull_stats();
+  stats_stale_ = true;
   return "";
 }
 
@@ -799,12 +797,23 @@ std::string Solver::dt_values(float* dt) {
   return "";
 }
 
-void Solver::stats(SolverStats& s) const { s = st_; }
+void Solver::stats(SolverStats& s) {
+  if (stats_stale_) pull_stats();
+  s = st_;
+}
 
 void Solver::reset_stats() {
-  st_ = SolverStats();
   cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 9, stream_);
   cudaStreamSynchronize(stream_);
+  // launch times recorded before the reset are dropped with the counters
+  auto& pend = prof_;
+  for (auto& pe : pend) {
+    cudaEventDestroy(pe.a);
+    cudaEventDestroy(pe.b);
+  }
+  pend.clear();
+  st_ = SolverStats();
+  stats_stale_ = false;
 }
 
 }  // namespace lsgb

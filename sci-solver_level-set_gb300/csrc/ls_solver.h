@@ -102,7 +102,7 @@ class Solver {
   std::string narrowband(unsigned char* flags);
   std::string active_patches(std::vector<int>& out);
   std::string dt_values(float* dt_new_order);
-  void stats(SolverStats& s) const;
+  void stats(SolverStats& s);  // reads the device counters if a step ran since the last read
   void reset_stats();
   int status_code() const { return status_; }
   void set_profile(bool on) { cfg_.profile = on ? 1 : 0; }
@@ -122,6 +122,15 @@ class Solver {
   std::string fim_loop(const StepParams& sp);
   std::string build_graph();
   void pull_stats();
+  bool stats_stale_ = false;  // device counters changed since the last pull_stats
+  // event pairs around the launches of profiled steps (cfg_.profile), read
+  // and released by pull_stats; kind 0 sweep, 1 check, 2 schedule, 3 seed,
+  // 4 narrowband, 5 update
+  struct ProfEvent {
+    cudaEvent_t a, b;
+    int kind;
+  };
+  std::vector<ProfEvent> prof_;
 
   const Layout* lay_ = nullptr;
   const KernelSet* K_ = nullptr;
