@@ -189,6 +189,8 @@ struct DeferredSolve {
   float res;
 };
 constexpr int kDeferCap = 1024;
+// words of k_fim_pair's shared seed mask (owned vertices per patch it covers: 32 x words)
+constexpr int kSeedMaskWords = 32;
 
 template <int D1>
 __device__ __forceinline__ void copy_metric(const DevMesh& m, long long c, float* Mt) {
@@ -715,6 +717,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
   __shared__ int s_li;    // list entry of the next patch
   __shared__ int s_ng;    // ghost-target solves listed when a check becomes a visit
+  __shared__ unsigned s_seed[kSeedMaskWords];  // seed flags of the owned vertices (bit i = vertex i)
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -738,6 +741,9 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   // fewer patches they add a visit's length to the iteration, while the next
   // sweep launch still waits for the patches that stayed active
   const bool early = CHECK && sp.niter > 1 && count >= 2 * (int)gridDim.x;
+  // the owned vertices' seed flags are kept in shared memory when every patch
+  // fits the mask (read by the check's verdict and the copy-out)
+  const bool seed_mask = sp.lvp <= 32 * kSeedMaskWords;
   if (tid == 0) {
     s_n[0] = s_n[1] = 0;
     s_li = blockIdx.x;
@@ -754,11 +760,21 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
       for (int i = tid; i < nvp + ngp; i += blockDim.x)
         sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
+      // whole warps run each 32-vertex word (the block is whole warps and the
+      // bound a multiple of 32)
+      if (seed_mask)
+        for (int i = tid; i < ((nvp + 31) & ~31); i += blockDim.x) {
+          const unsigned b = __ballot_sync(0xffffffffu, i < nvp && s.seed[vs + i] != 0);
+          if ((i & 31) == 0) s_seed[i >> 5] = b;
+        }
       if (tid == 0) {
         s_min = 0x7f800000u;
         s_ng = 0;
       }
       __syncthreads();
+      auto is_seed = [&](int i) -> bool {
+        return seed_mask ? ((s_seed[i >> 5] >> (i & 31)) & 1u) != 0u : s.seed[vs + i] != 0;
+      };
   #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
@@ -787,6 +803,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
       // a check that finds its patch unconverged turns into that patch's visit
       int niter_p = niter;
       bool visit = !CHECK;
+      int check_con = 1;  // the verdict of a check that stays a check
       unsigned need[2] = {0u, 0u};
   #pragma unroll 1
       for (int it = 0; it < niter_p; ++it) {
@@ -851,8 +868,9 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
           // vertex drop by tol or more?
           int c0 = 1;
           for (int i = tid; i < nvp; i += blockDim.x)
-            if (!s.seed[vs + i]) c0 &= (sOld[i] - sT[i] < sp.tol) ? 1 : 0;
-          if (!__syncthreads_and(c0) && early) {
+            if (!is_seed(i)) c0 &= (sOld[i] - sT[i] < sp.tol) ? 1 : 0;
+          check_con = __syncthreads_and(c0);
+          if (!check_con && early) {
             // activated: the patch's visit in the next FIM iteration would read
             // the same DT (DT changes only in the copy-back after the sweeps), so
             // it runs here and the next sweep skips the patch.  This sweep was
@@ -893,6 +911,8 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         }
         // refresh this thread's copies: owned vertices from the per-vertex
         // minimum, ghost vertices from this sweep's own result where solved
+        // (not after the last sweep: only the owned values are read then)
+        if (it == niter_p - 1) break;
   #pragma unroll
         for (int j = 0; j < 2; ++j) {
           const int c = tid + j * blockDim.x;
@@ -926,20 +946,22 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
         s_n[0] = s_n[1] = 0;  // read by every thread before the barrier above
         drawn = atomicAdd(next, 1);
       }
-      int con = 1;
-      for (int i = tid; i < nvp; i += blockDim.x) {
-        const int v = vs + i;
-        const float nt = sT[i];
-        float outv;
-        if (!s.seed[v]) {
-          if (visit) s.DT_out[v] = nt;
-          con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
-          outv = nt;
-        } else {
-          outv = s.DT[v];
+      // a check that stayed a check keeps its verdict: it writes no values
+      int con = visit ? 1 : check_con;
+      if (visit)
+        for (int i = tid; i < nvp; i += blockDim.x) {
+          const int v = vs + i;
+          const float nt = sT[i];
+          float outv;
+          if (!is_seed(i)) {
+            s.DT_out[v] = nt;
+            con &= (sOld[i] - nt < sp.tol) ? 1 : 0;
+            outv = nt;
+          } else {
+            outv = s.DT[v];
+          }
+          atomicMin(&s_min, __float_as_uint(outv));
         }
-        if (visit) atomicMin(&s_min, __float_as_uint(outv));
-      }
       if (tid == 0) {
         if (drawn == count - 1) atomicExch(next, 0);
         s_li = (int)gridDim.x + drawn;
