@@ -767,21 +767,16 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
           const unsigned b = __ballot_sync(0xffffffffu, i < nvp && s.seed[vs + i] != 0);
           if ((i & 31) == 0) s_seed[i >> 5] = b;
         }
-      if (tid == 0) {
-        s_min = 0x7f800000u;
-        s_ng = 0;
-      }
-      __syncthreads();
-      auto is_seed = [&](int i) -> bool {
-        return seed_mask ? ((s_seed[i >> 5] >> (i & 31)) & 1u) != 0u : s.seed[vs + i] != 0;
-      };
+      // the copies' connectivity, metric, heights and flags do not depend on
+      // the values, so their loads overlap the value gathers above (the
+      // previous patch's last reads of these arrays came before its final
+      // barrier)
   #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         if (c < nep) {
           const ushort4 cv = m.conn[es + c];
           sC[c] = cv;
-          sTc[c] = make_float4(sT[cv.x], sT[cv.y], sT[cv.z], sT[cv.w]);
           float Mt[11];
           copy_metric<4>(m, (long long)es + c, Mt);
           sM[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
@@ -798,6 +793,24 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
           const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
                                  (cv.w >= nvp ? 8u : 0u);
           sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
+        }
+      }
+      if (tid == 0) {
+        s_min = 0x7f800000u;
+        s_ng = 0;
+      }
+      __syncthreads();
+      auto is_seed = [&](int i) -> bool {
+        return seed_mask ? ((s_seed[i >> 5] >> (i & 31)) & 1u) != 0u : s.seed[vs + i] != 0;
+      };
+      // each thread's copies' values at the first sweep (read by the listing of
+      // the same thread, and by all solves after the listing's barrier)
+  #pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int c = tid + j * blockDim.x;
+        if (c < nep) {
+          const ushort4 cv = sC[c];
+          sTc[c] = make_float4(sT[cv.x], sT[cv.y], sT[cv.z], sT[cv.w]);
         }
       }
       // a check that finds its patch unconverged turns into that patch's visit
