@@ -188,7 +188,12 @@ ls_status ls_step_host(ls_handle* h, const float* phi_in, float* phi_out);
 ls_status ls_eikonal(ls_handle* h, const int* seeds, const float* values, int nseeds, float* dist);
 /* Current phi in the caller's vertex order. */
 ls_status ls_get_phi(ls_handle* h, float* phi);
+/* Work counters and profiled kernel times since the last ls_reset_stats.
+ * The device-side counters are read here (one small copy and a wait on the
+ * handle's stream when a step ran since the previous read), not after every
+ * step. */
 ls_status ls_get_stats(ls_handle* h, ls_stats* s);
+/* Zeroes the counters and drops profiled kernel times not yet read. */
 ls_status ls_reset_stats(ls_handle* h);
 /* Turn per-kernel CUDA-event timing on or off for the following steps
  * (kernels are then launched one by one instead of from the graph). */
