@@ -242,6 +242,30 @@ def test_graph_and_launch_paths_agree():
     assert sb["n_sweep"] > 0 and sb["ms_sweep"] > 0
 
 
+def test_profiled_launch_counts_belong_to_their_handle():
+    # profiled kernel times are kept per handle and read when stats are asked
+    # for: two handles stepped in turn report what each reports alone, and a
+    # reset drops times that were not read yet
+    keys = ("n_sweep", "n_check", "n_schedule", "n_seed", "n_narrowband", "n_update", "fim_iters", "patch_visits")
+    wa, wb = synth.workload("c3", n=12), synth.workload("c2", n=10)
+    alone = {}
+    for name, w in (("a", wa), ("b", wb)):
+        ls = lsgb300.from_workload(w, profile=True)
+        ls.step(2)
+        alone[name] = {k: ls.stats()[k] for k in keys}
+    a = lsgb300.from_workload(wa, profile=True)
+    b = lsgb300.from_workload(wb, profile=True)
+    for _ in range(2):
+        a.step(1)
+        b.step(1)
+    assert {k: a.stats()[k] for k in keys} == alone["a"]
+    assert {k: b.stats()[k] for k in keys} == alone["b"]
+    a.step(1)
+    a.reset_stats()
+    sa = a.stats()
+    assert sa["n_sweep"] == 0 and sa["ms_sweep"] == 0 and sa["patch_visits"] == 0
+
+
 def test_history_row0_is_phi0_and_default_inputs():
     w = synth.workload("c2", n=6)
     ls = lsgb300.from_workload(w)
