@@ -247,21 +247,6 @@ __global__ void k_loop_cond(const int* counts, int* ctl, cudaGraphConditionalHan
     cudaGraphSetConditional(h, (more && b < max_bodies) ? 1u : 0u);
   }
 }
-// n floats src -> dst (either side may be host memory that the GPU can
-// access); 16-byte vectors when both are aligned.
-__global__ void k_copy_f32(const float* __restrict__ src, float* __restrict__ dst, int n) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
-    const int n4 = n >> 2;
-    const float4* s4 = reinterpret_cast<const float4*>(src);
-    float4* d4 = reinterpret_cast<float4*>(dst);
-    for (int i = tid; i < n4; i += stride) d4[i] = s4[i];
-    for (int i = (n4 << 2) + tid; i < n; i += stride) dst[i] = src[i];
-  } else {
-    for (int i = tid; i < n; i += stride) dst[i] = src[i];
-  }
-}
-
 // After the narrowband: the next step's seed search is restricted to it
 // when it is not empty.
 __global__ void k_step_tail(const int* counts, int* ctl) {
@@ -678,24 +663,24 @@ std::string Solver::step_host(const float* phi_in, float* phi_out) {
   const int nv = m_.nv;
   if (pageable_) {
     // the GPU reads and writes the caller's pageable host arrays directly
-    // (coherent access over the CPU-GPU link): no host-side staging copy
-    k_copy_f32<<<L_.flat_grid, 256, 0, stream_>>>(phi_in, d_tmp_, nv);
-    LS_TRY(cudaGetLastError(), "copy in");
+    // (coherent access over the CPU-GPU link): the permutation kernels read
+    // and write the caller's side in its order (coalesced) and scatter or
+    // gather on the device side, with no staging copy on either side
+    LS_TRY(K_->permute(m_, phi_in, s_.phi, L_, stream_), "permute in");
   } else {
     std::memcpy(h_stage_, phi_in, sizeof(float) * nv);
     LS_TRY(cudaMemcpyAsync(d_tmp_, h_stage_, sizeof(float) * nv, cudaMemcpyHostToDevice, stream_), "h2d");
+    LS_TRY(K_->permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
   }
-  LS_TRY(K_->permute(m_, d_tmp_, s_.phi, L_, stream_), "permute");
-  st_.kernel_launches += pageable_ ? 4 : 2;  // (copy in,) permute, unpermute (, copy out)
+  st_.kernel_launches += 2;  // permute, unpermute
   bool empty = false;
   std::string r = one_step(&empty);
   if (!r.empty()) return r;
-  LS_TRY(K_->unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
   if (pageable_) {
-    k_copy_f32<<<L_.flat_grid, 256, 0, stream_>>>(d_tmp_, phi_out, nv);
-    LS_TRY(cudaGetLastError(), "copy out");
+    LS_TRY(K_->unpermute(m_, s_.phi, phi_out, L_, stream_), "unpermute out");
     LS_TRY(cudaStreamSynchronize(stream_), "sync");
   } else {
+    LS_TRY(K_->unpermute(m_, s_.phi, d_tmp_, L_, stream_), "unpermute");
     LS_TRY(cudaMemcpyAsync(h_stage_, d_tmp_, sizeof(float) * nv, cudaMemcpyDeviceToHost, stream_), "d2h");
     LS_TRY(cudaStreamSynchronize(stream_), "sync");
     std::memcpy(phi_out, h_stage_, sizeof(float) * nv);
