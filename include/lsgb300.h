@@ -230,10 +230,17 @@ enum {
  * the reference: it is the solver's narrowband kernel (narrowband patches,
  * phi = +-DT * scale, vertex-update count) for callers that cannot call
  * cudaMalloc -- host applications that own all device memory through their
- * own pool, fixed memory budgets, steps recorded once and replayed.  All
- * pointers except `counts` are device pointers owned by the caller:
- *   vert_offsets  nparts+1 ints, patch ranges of the vertices (layout order)
- *   dt            nv floats, FIM distances in the FIM frame
+ * own pool, or that run under a fixed device-memory budget, so that an
+ * allocation inside the call would take memory already handed out or fail.
+ * All pointers except `counts` are device pointers owned by the caller:
+ *   vert_offsets  nparts+1 ints, patch ranges of the vertices (layout
+ *                 order); must start at 0, never decrease and end at most at
+ *                 nv (the offsets live on the device and are not checked:
+ *                 other values make the kernel read and write outside dt,
+ *                 sign and phi)
+ *   dt            nv floats, FIM distances in the FIM frame (any value;
+ *                 the patch minimum compares them as floats, -0.0 and
+ *                 negative values included)
  *   sign          nv bytes, 1 where phi >= 0 before the redistance
  *   phi           nv floats, output: +-DT * scale (+-DT where DT >= largenum)
  *   nb_flags      nparts bytes, output: 1 for narrowband patches

@@ -8,7 +8,9 @@ in oracle/ref_shim/, directly from the reference tree (read-only):
                  (+ src/core3d/cuda/redistance3d.cu, which it links against)
 Nothing is copied out of the reference tree; outputs go only to oracle/_ref/.
 
-Usage: python oracle/build_ref.py [REFERENCE_ROOT]   (default /root/reference)
+Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+REFERENCE_ROOT defaults to the LS_REFERENCE_ROOT environment variable, else
+/root/reference; without a reference tree nothing is built.
 Constants the reference takes from its missing dependency: LARGENUM = 1e9,
 SMALLNUM = 1e-5 (the value src/core2d/include/redistance.h:17-19 uses).
 """
@@ -36,8 +38,12 @@ def run(cmd):
         raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
 
 
-def build(ref_root="/root/reference"):
-    src = os.path.join(ref_root, "src")
+def default_root():
+    return os.environ.get("LS_REFERENCE_ROOT", "/root/reference")
+
+
+def build(ref_root=None):
+    src = os.path.join(ref_root or default_root(), "src")
     if not os.path.isdir(src):
         return False
     os.makedirs(OUT, exist_ok=True)
@@ -66,5 +72,5 @@ def build(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    ok = build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ok = build(sys.argv[1] if len(sys.argv) > 1 else None)
     print("built" if ok else "reference tree not found; nothing built")

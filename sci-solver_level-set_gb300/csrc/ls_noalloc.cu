@@ -2,9 +2,10 @@
 //
 // For callers that cannot call cudaMalloc (or any allocating library
 // routine) on the device they run on: a host application that owns every
-// device allocation through its own pool, code running under a fixed
-// memory budget, or a step recorded once and replayed, where an allocation
-// inside the call is not allowed.  They keep their own device buffers for
+// device allocation through its own pool, or code running under a fixed
+// memory budget, where an allocation inside the call is not allowed (it
+// would take memory the caller has already handed out, or fail once the
+// budget is spent).  They keep their own device buffers for
 // the inputs and outputs; the kernel's scratch (the compact list of
 // narrowband patches and the counters) lives in the file-scope device array
 // below, sized for at most LS_NOALLOC_MAX_PATCHES patches.
@@ -36,10 +37,23 @@ static __device__ __align__(256) int g_nb_scratch[kCounters + kMaxPatches];
 std::mutex g_mu;
 int* g_scratch_ptr[kMaxDevices] = {nullptr};
 
+// Float bits -> unsigned key with the same order as the floats (negative
+// values, -0.0 included, rank below +0.0), and back.  For dt >= +0 the key
+// order is the bit order the solver's narrowband kernel compares.
+__device__ __forceinline__ unsigned order_key(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float order_key_value(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
 // Same selection as the solver's narrowband kernel: a patch is in the
 // narrowband when the minimum distance of its owned vertices is at most the
 // bandwidth; phi = +-DT * scale (+-DT when DT >= largenum); vertices with
-// DT <= bandwidth are counted as vertex updates.
+// DT <= bandwidth are counted as vertex updates.  The minimum is taken over
+// order keys, so any dt the caller passes (negative values and -0.0 too)
+// ranks as the floats do.
 __global__ void k_narrowband_noalloc(int nparts, const int* __restrict__ vert_off, const float* __restrict__ dt,
                                      const uint8_t* __restrict__ sign, float bandwidth, float scale,
                                      float largenum, float* __restrict__ phi, int* scratch) {
@@ -52,16 +66,16 @@ __global__ void k_narrowband_noalloc(int nparts, const int* __restrict__ vert_of
   unsigned cnt = 0, pv = 0;
   for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < nparts; p += nwarps) {
     const int vs = vert_off[p], ve = vert_off[p + 1];
-    unsigned mn = 0x7f800000u;
+    unsigned mn = order_key(__int_as_float(0x7f800000));
     for (int v = vs + lane; v < ve; v += 32) {
       const float d = dt[v];
-      mn = min(mn, __float_as_uint(d));
+      mn = min(mn, order_key(d));
       cnt += (d <= bandwidth);
       const float mag = (d >= largenum || scale == 1.f) ? d : d * scale;
       phi[v] = sign[v] ? mag : -mag;
     }
     mn = __reduce_min_sync(0xffffffffu, mn);
-    if (lane == 0 && __uint_as_float(mn) <= bandwidth) {
+    if (lane == 0 && order_key_value(mn) <= bandwidth) {
       const int pos = atomicAdd(&scratch[0], 1);
       list[pos] = p;
       pv += ve - vs;

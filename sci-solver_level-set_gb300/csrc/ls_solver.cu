@@ -51,7 +51,51 @@ Solver::~Solver() {
     cudaEventDestroy(pe.a);
     cudaEventDestroy(pe.b);
   }
+  for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
+}
+
+// Two events for one profiled launch, from the pool where it has some.
+cudaError_t Solver::prof_begin(ProfEvent& pe, int kind) {
+  pe.kind = kind;
+  cudaEvent_t ev[2];
+  for (int i = 0; i < 2; ++i) {
+    if (!ev_pool_.empty()) {
+      ev[i] = ev_pool_.back();
+      ev_pool_.pop_back();
+    } else {
+      cudaError_t e = cudaEventCreate(&ev[i]);
+      if (e != cudaSuccess) {
+        if (i == 1) ev_pool_.push_back(ev[0]);
+        return e;
+      }
+    }
+  }
+  pe.a = ev[0];
+  pe.b = ev[1];
+  return cudaSuccess;
+}
+
+// Adds the pending launch times to the stats (keep_times) or drops them, and
+// returns their events to the pool.
+void Solver::fold_prof(bool keep_times) {
+  for (auto& pe : prof_) {
+    float ms = 0;
+    if (keep_times && cudaEventSynchronize(pe.b) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, pe.a, pe.b) == cudaSuccess) {
+      switch (pe.kind) {
+        case 0: st_.ms_sweep += ms; st_.n_sweep++; break;
+        case 1: st_.ms_check += ms; st_.n_check++; break;
+        case 2: st_.ms_schedule += ms; st_.n_schedule++; break;
+        case 3: st_.ms_seed += ms; st_.n_seed++; break;
+        case 4: st_.ms_narrowband += ms; st_.n_narrowband++; break;
+        case 5: st_.ms_update += ms; st_.n_update++; break;
+      }
+    }
+    ev_pool_.push_back(pe.a);
+    ev_pool_.push_back(pe.b);
+  }
+  prof_.clear();
 }
 
 std::string Solver::check(cudaError_t e, const char* what) {
@@ -328,11 +372,10 @@ std::string Solver::fim_loop(const StepParams& sp) {
   auto prof = [&](int kind, auto&& fn) -> cudaError_t {
     if (!cfg_.profile) return fn();
     ProfEvent pe;
-    pe.kind = kind;
-    cudaEventCreate(&pe.a);
-    cudaEventCreate(&pe.b);
+    cudaError_t e = prof_begin(pe, kind);
+    if (e != cudaSuccess) return e;
     cudaEventRecord(pe.a, stream_);
-    cudaError_t e = fn();
+    e = fn();
     cudaEventRecord(pe.b, stream_);
     prof_.push_back(pe);
     return e;
@@ -362,11 +405,10 @@ std::string Solver::one_step(bool* empty_nb) {
   auto prof = [&](int kind, auto&& fn) -> cudaError_t {
     if (!cfg_.profile) return fn();
     ProfEvent pe;
-    pe.kind = kind;
-    cudaEventCreate(&pe.a);
-    cudaEventCreate(&pe.b);
+    cudaError_t e = prof_begin(pe, kind);
+    if (e != cudaSuccess) return e;
     cudaEventRecord(pe.a, stream_);
-    cudaError_t e = fn();
+    e = fn();
     cudaEventRecord(pe.b, stream_);
     prof_.push_back(pe);
     return e;
@@ -608,22 +650,7 @@ void Solver::pull_stats() {
   st_.sweep_slab_bytes = (long long)h_stats_[7];
   st_.flagged_copies = (long long)h_stats_[6];
   st_.early_visits = (long long)h_stats_[8];
-  auto& pend = prof_;
-  for (auto& pe : pend) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, pe.a, pe.b);
-    switch (pe.kind) {
-      case 0: st_.ms_sweep += ms; st_.n_sweep++; break;
-      case 1: st_.ms_check += ms; st_.n_check++; break;
-      case 2: st_.ms_schedule += ms; st_.n_schedule++; break;
-      case 3: st_.ms_seed += ms; st_.n_seed++; break;
-      case 4: st_.ms_narrowband += ms; st_.n_narrowband++; break;
-      case 5: st_.ms_update += ms; st_.n_update++; break;
-    }
-    cudaEventDestroy(pe.a);
-    cudaEventDestroy(pe.b);
-  }
-  pend.clear();
+  fold_prof(true);
 }
 
 std::string Solver::run(int nsteps, float* history, int* steps_done) {
@@ -639,6 +666,7 @@ std::string Solver::run(int nsteps, float* history, int* steps_done) {
     bool empty = false;
     std::string r = one_step(&empty);
     if (!r.empty()) return r;
+    if (cfg_.profile) fold_prof(true);
     if (empty) break;
     done++;
     if (history) {
@@ -676,6 +704,7 @@ std::string Solver::step_host(const float* phi_in, float* phi_out) {
   bool empty = false;
   std::string r = one_step(&empty);
   if (!r.empty()) return r;
+  if (cfg_.profile) fold_prof(true);
   if (pageable_) {
     LS_TRY(K_->unpermute(m_, s_.phi, phi_out, L_, stream_), "unpermute out");
     LS_TRY(cudaStreamSynchronize(stream_), "sync");
@@ -730,6 +759,7 @@ std::string Solver::eikonal(const int* seeds, const float* values, int nseeds, f
   sp.bandwidth = LN;
   std::string r = fim_loop(sp);
   if (!r.empty()) return r;
+  if (cfg_.profile) fold_prof(true);
   LS_TRY(cudaMemcpyAsync(dt.data(), s_.DT, sizeof(float) * nv, cudaMemcpyDeviceToHost, stream_), "d2h");
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   for (int v = 0; v < nv; ++v) out[L.vert_permute[v]] = (dt[v] >= LN) ? LN : dt[v] * sp_.scale;
@@ -791,12 +821,7 @@ void Solver::reset_stats() {
   cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 9, stream_);
   cudaStreamSynchronize(stream_);
   // launch times recorded before the reset are dropped with the counters
-  auto& pend = prof_;
-  for (auto& pe : pend) {
-    cudaEventDestroy(pe.a);
-    cudaEventDestroy(pe.b);
-  }
-  pend.clear();
+  fold_prof(false);
   st_ = SolverStats();
   stats_stale_ = false;
 }

@@ -123,14 +123,18 @@ class Solver {
   std::string build_graph();
   void pull_stats();
   bool stats_stale_ = false;  // device counters changed since the last pull_stats
-  // event pairs around the launches of profiled steps (cfg_.profile), read
-  // and released by pull_stats; kind 0 sweep, 1 check, 2 schedule, 3 seed,
-  // 4 narrowband, 5 update
+  // event pairs around the launches of profiled steps (cfg_.profile); kind 0
+  // sweep, 1 check, 2 schedule, 3 seed, 4 narrowband, 5 update.  Each
+  // profiled step folds its pairs into the stats when it ends and returns
+  // the events to a pool, so the number of events stays that of one step.
   struct ProfEvent {
     cudaEvent_t a, b;
     int kind;
   };
   std::vector<ProfEvent> prof_;
+  std::vector<cudaEvent_t> ev_pool_;
+  cudaError_t prof_begin(ProfEvent& pe, int kind);
+  void fold_prof(bool keep_times);
 
   const Layout* lay_ = nullptr;
   const KernelSet* K_ = nullptr;

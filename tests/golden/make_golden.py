@@ -4,8 +4,8 @@ Runs only where the reference tree is present and oracle/_ref has been built
 (python oracle/build_ref.py): the reference's own local solvers and host
 curvature update, compiled from its sources, are evaluated on seeded inputs
 and their outputs saved as small .npz fixtures.  The tests compare the
-oracle against these files, so the GPU machine (which has no reference tree)
-checks the oracle against the reference too.
+oracle against these files, so that a machine without the reference tree
+also checks the oracle against the reference.
 
     python tests/golden/make_golden.py
 """

@@ -1,0 +1,151 @@
+"""GPU parity on the benchmark configurations themselves and on the
+reference's own test meshes, through the C ABI against the CPU oracle.
+
+  * 2D advection, 64x64 cells (4,225 vertices), 20 steps, and 3D advection,
+    32^3 cells (35,937 vertices), 100 steps: the bit-exact build equals the
+    oracle bit for bit at every step (phi, narrowband patch set, work
+    counters); the fast build's max |phi - phi_FP64| over the band is
+    printed for every step and held to 1e-3 h (2D) or, for the 3D advection,
+    to the sensitivity of the FP64 oracle itself: the reference's update
+    drops elements whose residual |H| <= 1e-8 (meshFIM_kernels.h:161-273), a
+    discontinuity in phi, so the FP64 oracle started from phi0 perturbed by
+    1e-5 h per vertex drifts from the unperturbed run; the fast build must
+    stay within max(1e-3 h, that drift) over the 100 steps;
+  * 3D mean-curvature flow at full size, 128^3 cells (2,146,689 vertices):
+    the bit-exact build equals the oracle bit for bit over 2 steps, and the
+    fast build stays within 1e-3 h of the oracle run in FP64 over 3 steps;
+  * the reference's own meshes (src/test/test_data: sphere334, torus,
+    pyramid, SquareMesh_size16, sphere_266verts; committed fixtures), with
+    the inputs LevelSet::solveLevelSet uses when the caller sets none
+    (src/LevelSet.cu:187-233) and the default parameters, graph-partitioned
+    into 16-vertex patches as the reference's METIS path: the bit-exact
+    build equals the oracle bit for bit over 3 steps, in both modes.
+"""
+import numpy as np
+import pytest
+
+import lsgb300
+import lsoracle
+import ref_fixtures
+import synth
+
+pytestmark = pytest.mark.gpu
+
+COUNTERS = ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates", "nb_patches", "nb_patch_vertices")
+
+
+def _oracle(w, nsteps, precision=32, phi0=None, ref_compat=False):
+    ol = lsoracle.OracleLayout(w["dim"], w["xyz"], w["elems"], w["npart"], w["nparts"])
+    p = ol.params(update_kind=lsoracle.UPDATE[w["update"]], dt=w["dt"], bandwidth=w["bandwidth"],
+                  curv_coeff=1.0, ref_compat=1 if ref_compat else 0, precision=precision)
+    return ol.solve(p, w["phi0"] if phi0 is None else phi0, w["vel"], nsteps)
+
+
+def _band_max_err(a, b, bw, h):
+    band = (np.abs(a) <= bw) & (np.abs(b) <= bw)
+    assert band.sum() > 0
+    return float(np.max(np.abs(a[band].astype(np.float64) - b[band])) / h)
+
+
+def _bitexact_every_step(w, nsteps, ref_compat=False):
+    """Steps the bit-exact build one step at a time and compares phi, the
+    narrowband patch set and the work counters with the oracle after each."""
+    ref, nbs, _, ost = _oracle(w, nsteps, ref_compat=ref_compat)
+    assert ost["steps_run"] == nsteps
+    ls = lsgb300.from_workload(w, bit_exact=True, ref_compat=ref_compat)
+    for s in range(nsteps):
+        ls.step(1)
+        assert np.array_equal(ls.phi().view(np.uint32), ref[s + 1].view(np.uint32)), s
+        assert np.array_equal(ls.narrowband(w["nparts"]), nbs[s]), s
+    st = ls.stats()
+    for k in COUNTERS:
+        assert st[k] == ost[k], k
+
+
+def _fast_errors(w, nsteps):
+    ref64, _, _, o64 = _oracle(w, nsteps, precision=64)
+    assert o64["steps_run"] == nsteps
+    ls = lsgb300.from_workload(w)
+    hist, done = ls.solve(nsteps)
+    assert done == nsteps
+    return [_band_max_err(hist[s], ref64[s], w["bandwidth"], w["h"]) for s in range(1, nsteps + 1)], ref64
+
+
+def test_c1_2d_advection_64_cells_20_steps():
+    w = synth.workload("c1", n=64)
+    assert len(w["xyz"]) == 4225 and len(w["elems"]) == 8192
+    _bitexact_every_step(w, 20)
+    errs, _ = _fast_errors(w, 20)
+    print("C1 64^2 fast build max |phi - phi_FP64| / h per step:", " ".join("%.2e" % e for e in errs))
+    assert max(errs) <= 1e-3, errs
+
+
+def test_c2_3d_advection_32_cells_100_steps():
+    w = synth.workload("c2", n=32)
+    assert len(w["xyz"]) == 35937 and len(w["elems"]) == 196608
+    _bitexact_every_step(w, 100)
+    errs, ref64 = _fast_errors(w, 100)
+    # sensitivity of the FP64 oracle to a 1e-5 h perturbation of phi0
+    rng = np.random.default_rng(7)
+    phi_p = (w["phi0"].astype(np.float64) + 1e-5 * w["h"] * rng.choice([-1.0, 1.0], len(w["phi0"])))
+    pert, _, _, op = _oracle(w, 100, precision=64, phi0=phi_p.astype(np.float32))
+    assert op["steps_run"] == 100
+    drift = [_band_max_err(pert[s], ref64[s], w["bandwidth"], w["h"]) for s in range(1, 101)]
+    print("C2 32^3 fast build max |phi - phi_FP64| / h per step:", " ".join("%.2e" % e for e in errs))
+    print("C2 32^3 FP64 oracle drift from a 1e-5 h phi0 perturbation:", " ".join("%.2e" % e for e in drift))
+    print("C2 32^3 max fast error %.3e h, max FP64 drift %.3e h" % (max(errs), max(drift)))
+    assert max(errs) <= max(1e-3, max(drift)), (max(errs), max(drift))
+
+
+def test_c3_curvature_128_cells_full_size():
+    w = synth.workload("c3", n=128)
+    assert len(w["xyz"]) == 2146689 and len(w["elems"]) == 12582912
+    ref, nbs, _, ost = _oracle(w, 2)
+    ex = lsgb300.from_workload(w, bit_exact=True)
+    for s in range(2):
+        ex.step(1)
+        assert np.array_equal(ex.phi().view(np.uint32), ref[s + 1].view(np.uint32)), s
+        assert np.array_equal(ex.narrowband(w["nparts"]), nbs[s]), s
+    st = ex.stats()
+    for k in COUNTERS:
+        assert st[k] == ost[k], k
+    ex.close()
+    errs, _ = _fast_errors(w, 3)
+    print("C3 128^3 fast build max |phi - phi_FP64| / h per step:", " ".join("%.2e" % e for e in errs))
+    assert max(errs) <= 1e-3, errs
+
+
+def _fixture_case(name):
+    xyz, el, _ = ref_fixtures.load(name)
+    dim = 3 if el.shape[1] == 4 else 2
+    if dim == 3:
+        el = synth.reorient(xyz, el)  # the loader's orientation rule
+    npart, nparts = lsgb300.partition_graph(dim, el, len(xyz), 16)
+    return dim, xyz, el, npart, nparts
+
+
+@pytest.mark.parametrize("name", ref_fixtures.TETGEN + ref_fixtures.PLY)
+@pytest.mark.parametrize("ref_compat", [False, True])
+def test_reference_meshes_step_like_oracle(name, ref_compat):
+    dim, xyz, el, npart, nparts = _fixture_case(name)
+    nsteps = 3
+    flags = lsgb300.BITEXACT | (lsgb300.REF_COMPAT if ref_compat else 0)
+    ls = lsgb300.LevelSet(dim == 2, lsgb300.default_params(flags=flags))
+    ls.set_mesh(xyz, el)
+    ls.set_partition(npart, nparts)
+    ls.setup()  # no phi, no velocity: the reference's defaults
+    hist, done = ls.solve(nsteps)
+    phi0, vel = ref_fixtures.default_inputs(dim, xyz, len(el))
+    np.testing.assert_array_equal(hist[0], phi0)
+    p0 = lsgb300.default_params()
+    ol = lsoracle.OracleLayout(dim, xyz, el, npart, nparts)
+    p = ol.params(update_kind=lsoracle.UPDATE["advect"], dt=p0.time_step, bandwidth=p0.bandwidth, curv_coeff=1.0,
+                  ref_compat=1 if ref_compat else 0)
+    ref, nbs, _, ost = ol.solve(p, phi0, vel, nsteps)
+    assert done == ost["steps_run"]
+    assert np.array_equal(hist.view(np.uint32), ref.view(np.uint32))
+    if done:
+        assert np.array_equal(ls.narrowband(nparts), nbs[done - 1])
+    st = ls.stats()
+    for k in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
+        assert st[k] == ost[k], k

@@ -5,6 +5,7 @@ import pytest
 
 import lsgb300
 import lsoracle
+import ref_fixtures
 import synth
 
 ARRAYS = list(lsgb300.REF_ARRAYS)
@@ -109,19 +110,9 @@ def test_patch_too_large_is_reported():
     assert e.value.code == lsgb300.LS_PATCH_TOO_LARGE
 
 
-def test_reference_fixture_meshes_if_present():
-    """The reference's own tetgen fixtures (read only where the reference
-    tree exists; skipped elsewhere)."""
-    import os
-
-    base = "/root/reference/src/test/test_data"
-    if not os.path.isdir(base):
-        pytest.skip("reference fixtures not present")
-    for name, target in (("sphere334", 16), ("torus", 16), ("pyramid", 3)):
-        node = np.loadtxt(os.path.join(base, name + ".node"), skiprows=1, comments="#")
-        ele = np.loadtxt(os.path.join(base, name + ".ele"), skiprows=1, comments="#", dtype=np.int64)
-        xyz = node[:, 1:4].astype(np.float32)
-        first = int(node[0, 0])
-        el = (ele[:, 1:5] - first).astype(np.int32)
-        npart, nparts = lsgb300.partition_rcb(3, xyz, target)
-        _compare(3, xyz, el, npart, nparts)
+@pytest.mark.parametrize("name,target", [("sphere334", 16), ("torus", 16), ("pyramid", 3)])
+def test_reference_fixture_meshes(name, target):
+    """The reference's own tetgen meshes (committed fixtures), RCB-partitioned."""
+    xyz, el, _ = ref_fixtures.load(name)
+    npart, nparts = lsgb300.partition_rcb(3, xyz, target)
+    _compare(3, xyz, el, npart, nparts)

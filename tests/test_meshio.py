@@ -8,9 +8,8 @@ import pytest
 
 import lsgb300
 import lsoracle
+import ref_fixtures
 import synth
-
-REF_DATA = "/root/reference/src/test/test_data"
 
 
 def _parse_tetgen(base):
@@ -150,43 +149,69 @@ def test_bad_files(tmp_path):
         lsgb300.LevelSet(True).load_mesh(p)
 
 
-def _have(name):
-    return os.path.exists(os.path.join(REF_DATA, name))
+def _ref_file(name):
+    d = ref_fixtures.reference_data_dir()
+    if d is None or not os.path.exists(os.path.join(d, name)):
+        pytest.skip("reference tree not given (LS_REFERENCE_ROOT)")
+    return os.path.join(d, name)
 
 
-@pytest.mark.parametrize("name", ["sphere334", "torus", "pyramid"])
+@pytest.mark.parametrize("name", ref_fixtures.TETGEN)
 def test_reference_tetgen_fixtures(name):
-    if not _have(name + ".node"):
-        pytest.skip("reference test data not present")
-    base = os.path.join(REF_DATA, name)
+    """The original files, where the reference tree is given: the loader's
+    result equals the committed fixture (reoriented)."""
+    base = _ref_file(name + ".node")[:-5]
     ls = lsgb300.LevelSet(False)
     x, t = ls.load_mesh(base)
     ex, et = _parse_tetgen(base)
+    fx, fe, _ = ref_fixtures.load(name)
+    assert np.array_equal(ex, fx) and np.array_equal(et, fe)
     assert np.array_equal(x, ex)
     assert np.array_equal(t, synth.reorient(ex, et))
 
 
-@pytest.mark.parametrize("name", ["SquareMesh_size16.ply", "sphere_266verts.ply", "sphere_1154verts.ply"])
+@pytest.mark.parametrize("name", ref_fixtures.PLY + ("sphere_1154verts",))
 def test_reference_ply_fixtures(name):
-    if not _have(name):
-        pytest.skip("reference test data not present")
-    path = os.path.join(REF_DATA, name)
+    path = _ref_file(name + ".ply")
     ls = lsgb300.LevelSet(True)
     x, t = ls.load_mesh(path)
     ex, et = _parse_ply(path)
     assert np.array_equal(x, ex) and np.array_equal(t, et)
+    if name in ref_fixtures.PLY:
+        fx, fe, _ = ref_fixtures.load(name)
+        assert np.array_equal(ex, fx) and np.array_equal(et, fe)
+
+
+@pytest.mark.parametrize("name", ref_fixtures.TETGEN + ref_fixtures.PLY)
+def test_fixture_meshes_through_loader(tmp_path, name):
+    """The reference's meshes (committed fixtures), written back in their
+    file format with the file's index base, load to the same arrays; tetgen
+    meshes come back with the loader's orientation fix-up applied."""
+    xyz, el, first = ref_fixtures.load(name)
+    if name in ref_fixtures.TETGEN:
+        base = str(tmp_path / name)
+        synth.write_tetgen(base, xyz, el, first=first)
+        x, t = lsgb300.LevelSet(False).load_mesh(base)
+        assert np.array_equal(t, synth.reorient(xyz, el))
+    else:
+        path = str(tmp_path / (name + ".ply"))
+        synth.write_ply(path, xyz, [tuple(r) for r in el])
+        x, t = lsgb300.LevelSet(True).load_mesh(path)
+        assert np.array_equal(t, el)
+    assert np.array_equal(x, xyz)
 
 
 def test_reference_fixture_layout_matches_oracle():
-    """The loaded sphere334 mesh, RCB-partitioned, gives the same patch layout
-    as the restatement of the reference's layout code."""
-    if not _have("sphere334.node"):
-        pytest.skip("reference test data not present")
+    """The reference's sphere334 mesh (committed fixture), oriented as the
+    loader leaves it and RCB-partitioned, gives the same patch layout as the
+    restatement of the reference's layout code."""
+    xyz, el, _ = ref_fixtures.load("sphere334")
+    t = synth.reorient(xyz, el)
     ls = lsgb300.LevelSet(False)
-    x, t = ls.load_mesh(os.path.join(REF_DATA, "sphere334"))
-    npart, nparts = lsgb300.partition_rcb(3, x, 16)
+    ls.set_mesh(xyz, t)
+    npart, nparts = lsgb300.partition_rcb(3, xyz, 16)
     ls.set_partition(npart, nparts)
     ls.prepare()
-    ol = lsoracle.OracleLayout(3, x, t, npart, nparts)
+    ol = lsoracle.OracleLayout(3, xyz, t, npart, nparts)
     for a in lsgb300.REF_ARRAYS:
         assert np.array_equal(ls.layout(a), ol.array(a)), a

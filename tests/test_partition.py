@@ -1,15 +1,12 @@
 """Partitioners behind partition_type: the graph partitioner (recursive graph
 bisection + refinement, the METIS stand-in), recursive coordinate bisection
 and GraphPartition_Square blocks."""
-import os
-
 import numpy as np
 import pytest
 
 import lsgb300
+import ref_fixtures
 import synth
-
-REF_DATA = "/root/reference/src/test/test_data"
 
 
 def _check(npart, nparts, nv, target, dim=3):
@@ -79,10 +76,8 @@ def test_handle_partition_types():
 
 
 def test_reference_mesh_graph_partition():
-    if not os.path.exists(os.path.join(REF_DATA, "torus.node")):
-        pytest.skip("reference test data not present")
-    ls = lsgb300.LevelSet(False)
-    xyz, el = ls.load_mesh(os.path.join(REF_DATA, "torus"))
+    # the reference's torus mesh (committed fixture)
+    xyz, el, _ = ref_fixtures.load("torus")
     pg, ng = lsgb300.partition_graph(3, el, len(xyz), 16)
     _check(pg, ng, len(xyz), 16)
     pr, _ = lsgb300.partition_rcb(3, xyz, 16)
