@@ -6,6 +6,12 @@ in oracle/ref_shim/, directly from the reference tree (read-only):
   libref_tri.so  localSolverTri, localSolverTet1 (src/core2d/include/redistance_kernels.h)
   libref_k20.so  meshFIM3d::updateT_single_stage from src/core3d/cuda/meshFIM3d.cu
                  (+ src/core3d/cuda/redistance3d.cu, which it links against)
+  libref_layout3d.so, libref_layout2d.so
+                 the patch layout (InitPatches, InitPatches2,
+                 GenerateBlockNeighbors, GraphPartition_Square) from
+                 src/core{3,2}d/cuda/meshFIM{3,2}d.cu, linked without the CUDA
+                 runtime: oracle/ref_host_launch.cpp runs their layout kernels
+                 on the CPU (oracle/ref_harness_layout{3,2}d.cu drive them)
 Nothing is copied out of the reference tree; outputs go only to oracle/_ref/.
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
@@ -30,6 +36,13 @@ def nvcc():
         if os.path.sep not in c or os.path.exists(c):
             return c
     return "nvcc"
+
+
+def nvcc_path():
+    import shutil
+
+    c = nvcc()
+    return c if os.path.sep in c else (shutil.which(c) or "/usr/local/cuda/bin/nvcc")
 
 
 def run(cmd):
@@ -61,13 +74,31 @@ def build(ref_root=None):
         (base + inc3 + ["-DLSREF_HOST_ONLY", "-c", os.path.join(HERE, "ref_harness_k20.cu"),
                         "-o", os.path.join(OUT, "k20.o")]),
     ]
-    with ThreadPoolExecutor(max_workers=5) as ex:
+    o = lambda n: os.path.join(OUT, n)  # noqa: E731
+    host = ["-DLSREF_HOST_ONLY", "-c"]
+    jobs += [
+        (base + inc3 + host + [os.path.join(HERE, "ref_harness_layout3d.cu"), "-o", o("layout3d.o")]),
+        (base + inc2 + host + [os.path.join(HERE, "ref_harness_layout2d.cu"), "-o", o("layout2d.o")]),
+        (base + inc2 + host + [os.path.join(src, "core2d", "cuda", "meshFIM2d.cu"), "-o", o("meshFIM2d.o")]),
+        (base + inc2 + host + [os.path.join(src, "core2d", "cuda", "redistance.cu"), "-o", o("redistance2d.o")]),
+    ]
+    # the kernel-launch stand-ins, with the host compiler
+    gxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-I" + SHIM,
+           "-I" + os.path.join(os.path.dirname(os.path.dirname(nvcc_path())), "include")]
+    for d, inc in ((3, inc3), (2, inc2)):
+        jobs.append(gxx + inc + ["-DLSREF_DIM=%d" % d, "-c", os.path.join(HERE, "ref_host_launch.cpp"),
+                                 "-o", o("host_launch%dd.o" % d)])
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
     link = [nvcc(), "-shared"] + ARCH
-    run(link + [os.path.join(OUT, "tet.o"), "-o", os.path.join(OUT, "libref_tet.so")])
-    run(link + [os.path.join(OUT, "tri.o"), "-o", os.path.join(OUT, "libref_tri.so")])
-    run(link + [os.path.join(OUT, n) for n in ("k20.o", "meshFIM3d.o", "redistance3d.o")] +
-        ["-o", os.path.join(OUT, "libref_k20.so")])
+    run(link + [o("tet.o"), "-o", o("libref_tet.so")])
+    run(link + [o("tri.o"), "-o", o("libref_tri.so")])
+    run(link + [o(n) for n in ("k20.o", "meshFIM3d.o", "redistance3d.o")] + ["-o", o("libref_k20.so")])
+    # no CUDA runtime: every launch goes to the host stand-ins
+    run(["g++", "-shared", "-Wl,--no-undefined", "-o", o("libref_layout3d.so")] +
+        [o(n) for n in ("layout3d.o", "meshFIM3d.o", "redistance3d.o", "host_launch3d.o")])
+    run(["g++", "-shared", "-Wl,--no-undefined", "-o", o("libref_layout2d.so")] +
+        [o(n) for n in ("layout2d.o", "meshFIM2d.o", "redistance2d.o", "host_launch2d.o")])
     return True
 
 

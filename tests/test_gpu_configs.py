@@ -18,7 +18,8 @@ reference's own test meshes, through the C ABI against the CPU oracle.
     pyramid, SquareMesh_size16, sphere_266verts; committed fixtures), with
     the inputs LevelSet::solveLevelSet uses when the caller sets none
     (src/LevelSet.cu:187-233) and the default parameters, graph-partitioned
-    into 16-vertex patches as the reference's METIS path: the bit-exact
+    into 16-vertex patches as the reference's METIS path (the pyramid into
+    3-vertex patches): the bit-exact
     build equals the oracle bit for bit over 3 steps, in both modes.
 """
 import numpy as np
@@ -120,7 +121,10 @@ def _fixture_case(name):
     dim = 3 if el.shape[1] == 4 else 2
     if dim == 3:
         el = synth.reorient(xyz, el)  # the loader's orientation rule
-    npart, nparts = lsgb300.partition_graph(dim, el, len(xyz), 16)
+    # 16-vertex patches (the default metis size); the 7-vertex pyramid in
+    # 3-vertex patches, since one patch has no patch adjacency for the
+    # reference's block-neighbour construction to list
+    npart, nparts = lsgb300.partition_graph(dim, el, len(xyz), 3 if name == "pyramid" else 16)
     return dim, xyz, el, npart, nparts
 
 

@@ -1,10 +1,16 @@
-"""The oracle is pinned to the reference: its local solvers and its host
-curvature update reproduce the reference's own code (compiled from the
-reference sources into oracle/_ref; outputs committed in tests/golden/)."""
+"""The oracle and the product are pinned to the reference: the oracle's local
+solvers and host curvature update reproduce the reference's own code, and the
+product's patch layout builder and the oracle's restatement of it reproduce
+the layout the reference's own InitPatches / InitPatches2 /
+GenerateBlockNeighbors build (compiled from the reference sources into
+oracle/_ref; outputs committed in tests/golden/)."""
+import hashlib
 import os
 
 import numpy as np
+import pytest
 
+import lsgb300
 import lsoracle
 import synth
 
@@ -46,3 +52,55 @@ def test_curvature_update_matches_reference_host_function():
     moved = np.abs(out - phi)
     assert moved.max() > 1e-3
     np.testing.assert_allclose(mine, out, rtol=0, atol=2e-6 * max(1.0, float(np.abs(out).max())))
+
+
+def _layout_cases():
+    with np.load(os.path.join(GOLD, "ref_layout.npz")) as g:
+        return [str(c) for c in g["cases"]]
+
+
+class _Case:
+    """One case's entries of the layout golden file, keyed without the case
+    prefix."""
+
+    def __init__(self, d):
+        self._d = d
+        self.files = list(d)
+
+    def __getitem__(self, k):
+        return self._d[k]
+
+
+def _same(g, key, mine):
+    """Bit-exact comparison with the stored array, or with its length and
+    SHA-256 digest where only those are stored."""
+    mine = np.ascontiguousarray(mine)
+    if key in g.files:
+        ref = g[key]
+        if ref.dtype == np.float64:  # the 2D reference keeps local coordinates in double
+            ref = ref.astype(np.float32)
+        return mine.shape == ref.shape and np.array_equal(mine.view(np.uint8), ref.view(np.uint8))
+    return (mine.size == int(g[key + ":len"]) and
+            hashlib.sha256(mine.tobytes()).hexdigest() == str(g[key + ":sha256"]))
+
+
+@pytest.mark.parametrize("case", _layout_cases())
+def test_layout_equals_reference_layout(case):
+    with np.load(os.path.join(GOLD, "ref_layout.npz")) as z:
+        g = _Case({k.split(":", 1)[1]: z[k] for k in z.files if k.startswith(case + ":")})
+    dim = int(g["dim"])
+    xyz, el, npart, nparts = g["xyz"], g["elems"], g["npart"], int(g["nparts"])
+    if int(g["side"]) > 0:
+        # the reference's GraphPartition_Square labels = the structured partitioner's
+        mine, n = lsgb300.partition_structured(dim, int(g["side"]), int(g["block"]), len(xyz))
+        assert n == nparts and np.array_equal(mine, npart)
+    ls = lsgb300.LevelSet(dim == 2)
+    ls.set_mesh(xyz, el)
+    ls.set_partition(npart, nparts)
+    ls.prepare()
+    info = ls.layout_info()
+    assert info["nparts"] == nparts and info["full"] == int(g["full"]) and info["lep"] == int(g["lep"])
+    ol = lsoracle.OracleLayout(dim, xyz, el, npart, nparts)
+    for a in lsgb300.REF_ARRAYS:
+        assert _same(g, a, ls.layout(a).ravel()), (case, "product", a)
+        assert _same(g, a, ol.array(a).ravel()), (case, "oracle", a)
