@@ -10,9 +10,13 @@ in oracle/ref_shim/, directly from the reference tree (read-only):
                  the patch layout (InitPatches, InitPatches2,
                  GenerateBlockNeighbors, GraphPartition_Square) from
                  src/core{3,2}d/cuda/meshFIM{3,2}d.cu, linked without the CUDA
-                 runtime: oracle/ref_host_launch.cpp runs their layout kernels
-                 on the CPU (oracle/ref_harness_layout{3,2}d.cu drive them)
-Nothing is copied out of the reference tree; outputs go only to oracle/_ref/.
+                 runtime: oracle/ref_host_launch.cpp runs their kernels on the
+                 CPU (oracle/ref_harness_layout{3,2}d.cu drive them); the 3D
+                 library also runs the reference's whole time step
+                 (meshFIM3d::GenerateData, oracle/ref_harness_layout3d.cu)
+Nothing is copied into the repository; outputs go only to oracle/_ref/ (the
+host build of the kernels reads copies of the kernel headers written there
+with their dynamic shared-memory declaration pointed at a host buffer).
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
 REFERENCE_ROOT defaults to the LS_REFERENCE_ROOT environment variable, else
@@ -51,6 +55,33 @@ def run(cmd):
         raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
 
 
+# the declaration of the kernels' dynamic shared memory, and what the host
+# copies of the kernels (oracle/ref_host_launch.cpp) declare in its place
+DYN_SMEM_DECL = "extern __shared__ char s_array[];"
+DYN_SMEM_HOST = "char* s_array = dyn_smem;"
+HOST_HEADERS = {3: ["meshFIM_kernels.h", "redistance_kernels3d.h"], 2: ["meshFIM2d_kernels.h"]}
+
+
+def generate_host_headers(src):
+    """Copies of the reference's kernel headers into oracle/_ref/gen{3,2}d/
+    for the host build of the kernels, with one change: the dynamic
+    shared-memory declaration becomes a pointer to the host buffer (a C++
+    function cannot declare an extern array as a static).  Returns the
+    include directory per dimension."""
+    out = {}
+    for d, names in HOST_HEADERS.items():
+        gdir = os.path.join(OUT, "gen%dd" % d)
+        os.makedirs(gdir, exist_ok=True)
+        for name in names:
+            text = open(os.path.join(src, "core%dd" % d, "include", name)).read()
+            if DYN_SMEM_DECL not in text:
+                raise RuntimeError("%s: dynamic shared-memory declaration not found" % name)
+            with open(os.path.join(gdir, name), "w") as f:
+                f.write(text.replace(DYN_SMEM_DECL, DYN_SMEM_HOST))
+        out[d] = gdir
+    return out
+
+
 def default_root():
     return os.environ.get("LS_REFERENCE_ROOT", "/root/reference")
 
@@ -82,12 +113,15 @@ def build(ref_root=None):
         (base + inc2 + host + [os.path.join(src, "core2d", "cuda", "meshFIM2d.cu"), "-o", o("meshFIM2d.o")]),
         (base + inc2 + host + [os.path.join(src, "core2d", "cuda", "redistance.cu"), "-o", o("redistance2d.o")]),
     ]
-    # the kernel-launch stand-ins, with the host compiler
-    gxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-I" + SHIM,
+    # the kernel-launch stand-ins, with the host compiler, on the kernel
+    # headers as generate_host_headers leaves them
+    gen = generate_host_headers(src)
+    gxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-DSMALLNUM=1e-5", "-I" + SHIM,
            "-I" + os.path.join(os.path.dirname(os.path.dirname(nvcc_path())), "include")]
     for d, inc in ((3, inc3), (2, inc2)):
-        jobs.append(gxx + inc + ["-DLSREF_DIM=%d" % d, "-c", os.path.join(HERE, "ref_host_launch.cpp"),
-                                 "-o", o("host_launch%dd.o" % d)])
+        jobs.append(gxx + ["-I" + gen[d]] + inc + ["-DLSREF_DIM=%d" % d, "-c",
+                                                   os.path.join(HERE, "ref_host_launch.cpp"),
+                                                   "-o", o("host_launch%dd.o" % d)])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
     link = [nvcc(), "-shared"] + ARCH

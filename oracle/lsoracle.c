@@ -20,6 +20,8 @@
 #endif
 
 enum { LSO_SEED = 0, LSO_ACTIVE = 1, LSO_ALIVE = 2, LSO_FAR = 3 };
+/* per-vertex slots the reference's patch kernels keep (l_mem) */
+#define LSO_SLOT_CAP(dim) ((dim) == 3 ? 32 : 16)
 
 struct lso_layout {
   int dim, nv, ne, nparts, full, lep, lvp, lim, nadj;

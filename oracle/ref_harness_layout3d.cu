@@ -16,7 +16,18 @@
 #include <cstring>
 #include <vector>
 
-extern "C" void METIS_PartGraphKway(int*, int*, int*, int*, int*, int*, int*, int*, int*, int*, int*) {}
+// METIS stand-in for Partition_METIS: the labels lsref_metis_labels set
+// (nothing otherwise; the layout entry point sets the partition members)
+namespace {
+std::vector<int>& metis_labels() {
+  static std::vector<int> v;
+  return v;
+}
+}  // namespace
+extern "C" void METIS_PartGraphKway(int* nn, int*, int*, int*, int*, int*, int*, int*, int*, int*, int* part) {
+  const std::vector<int>& l = metis_labels();
+  if ((int)l.size() == *nn) std::memcpy(part, l.data(), sizeof(int) * l.size());
+}
 extern "C" int lsref_host_launches(int* unknown);
 extern "C" int lsref_host_ipermute(int* out, int n);
 
@@ -126,4 +137,56 @@ extern "C" long long lsref_layout3d_array(int which, void* dst) {
   }
   if (dst) std::memcpy(dst, v->data(), sizeof(int) * v->size());
   return (long long)v->size();
+}
+
+/*
+ * The reference's whole time-step loop, meshFIM3d::GenerateData
+ * (meshFIM3d.cu:572-690): partition (GraphPartition_Square for side > 0, else
+ * Partition_METIS with the given labels standing in for METIS' result),
+ * layout, then per step seed search, sign capture, FIM redistance
+ * (redistance3d.cu:67-274), narrowband and `inside_niter` advection updates
+ * (meshFIM3d.cu:83-99).  phi0: nv floats; vel: 3 floats per element (the
+ * TetMesh normals GenerateData reads as the element velocity).  history:
+ * (nsteps + 1) x nv floats, row 0 = phi0 (the rows GenerateData returns).
+ * Returns the number of steps run (GenerateData stops early on an empty
+ * narrowband), or a negative code.
+ */
+extern "C" void lsref_metis_labels(const int* npart, int nv) { metis_labels().assign(npart, npart + nv); }
+
+extern "C" int lsref_solve3d(int nv, const float* xyz, int ne, const int* tets, const int* ring_off, const int* ring,
+                             const int* npart, int nparts, int side, int block, const float* phi0, const float* vel,
+                             int nsteps, float dt, float bandwidth, int inside_niter, float* history) {
+  TetMesh mesh;
+  mesh.vertices.resize(nv);
+  for (int v = 0; v < nv; ++v) mesh.vertices[v] = point(xyz[3 * v], xyz[3 * v + 1], xyz[3 * v + 2]);
+  mesh.tets.resize(ne);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 4; ++k) mesh.tets[e][k] = tets[4 * e + k];
+  mesh.neighbors.resize(nv);
+  mesh.adjacenttets.resize(nv);
+  for (int v = 0; v < nv; ++v) mesh.neighbors[v].assign(ring + ring_off[v], ring + ring_off[v + 1]);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < 4; ++k) mesh.adjacenttets[tets[4 * e + k]].push_back(e);
+  mesh.vertT.assign(phi0, phi0 + nv);
+  mesh.normals.resize(ne);
+  for (int e = 0; e < ne; ++e) mesh.normals[e] = point(vel[3 * e], vel[3 * e + 1], vel[3 * e + 2]);
+  int part_type = 1, metis_size = 0;
+  if (side <= 0) {
+    // Partition_METIS makes ceil(nv / metis_size) parts: pick a size that
+    // gives the caller's part count
+    part_type = 0;
+    metis_size = (nv + nparts - 1) / nparts;
+    if ((nv + metis_size - 1) / metis_size != nparts) return -3;
+    lsref_metis_labels(npart, nv);
+  }
+  meshFIM3d fim(&mesh);
+  lsref_host_launches(nullptr);
+  std::vector<std::vector<float>> ans =
+      fim.GenerateData((char*)"", nsteps, dt, inside_niter, side, block, bandwidth, part_type, metis_size, false);
+  int failed = 0;
+  g_res.launches = lsref_host_launches(&failed);
+  if (failed) return -1;
+  for (size_t s = 0; s < ans.size(); ++s)
+    std::memcpy(history + s * (size_t)nv, ans[s].data(), sizeof(float) * nv);
+  return (int)ans.size() - 1;
 }

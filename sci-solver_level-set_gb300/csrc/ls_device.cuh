@@ -33,6 +33,12 @@ struct DevMesh {
   const float* sig;          // SoA [3][full] per-copy velocity (2D: projected, 2 rows)
   const int* vslot_off;      // nv+1
   const uint16_t* vslot;     // owned-vertex slots (copy_local*4 + k)
+  // per copy: corners beyond the reference's per-vertex slot limit, set only
+  // with the reference's semantics on meshes that have such corners (null
+  // otherwise): they stay private to their copy in the FIM sweep and are
+  // left out of the update's sums (Layout::slot_capped)
+  const uint8_t* capped;
+  int slot_cap;              // the limit: 32 (tetrahedra) or 16 (triangles)
   const int* padj_off;       // nparts+1
   const int* padj;           // patch adjacency
   const float* xyz;          // SoA [3][nv]

@@ -276,9 +276,16 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
     float T[4] = {0.f, 0.f, 0.f, 0.f};
     float Mt[11];
     int nflag = 0;
+    // corners whose value is the vertex's: owned, and within the reference's
+    // per-vertex slot limit where that applies (others stay private)
+    unsigned shared_k = 0u;
     if (act) {
       const ushort4 cv = m.conn[es + tid];
       idx[0] = cv.x; idx[1] = cv.y; idx[2] = cv.z; idx[3] = cv.w;
+      const unsigned capm = m.capped ? (unsigned)m.capped[es + tid] : 0u;
+#pragma unroll
+      for (int k = 0; k < D1; ++k)
+        if (idx[k] < nvp && !((capm >> k) & 1u)) shared_k |= 1u << k;
 #pragma unroll
       for (int k = 0; k < D1; ++k) T[k] = sT[idx[k]];
       copy_metric<D1>(m, (long long)es + tid, Mt);
@@ -320,7 +327,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
         }
 #pragma unroll
         for (int k = 0; k < D1; ++k) {
-          if (idx[k] < nvp) atomicMin(reinterpret_cast<int*>(&sT[idx[k]]), __float_as_int(nw[k]));
+          if ((shared_k >> k) & 1u) atomicMin(reinterpret_cast<int*>(&sT[idx[k]]), __float_as_int(nw[k]));
           else T[k] = nw[k];
         }
       }
@@ -335,7 +342,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
           const float res = fminf(e.t[k], solve_k_fp64(Mq, e.t, k, sp.eps_h64, sp.largenum));
           const ushort4 cv = m.conn[es + cl];
           const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
-          if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(res));
+          const bool capped_k = m.capped && ((m.capped[es + cl] >> k) & 1u);
+          if (tk < nvp && !capped_k) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(res));
           else e.res = res;
           nflag++;
         }
@@ -343,14 +351,14 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
         if (act) {
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (qpos[k] >= 0 && idx[k] >= nvp) T[k] = sQ[qpos[k]].res;
+            if (qpos[k] >= 0 && !((shared_k >> k) & 1u)) T[k] = sQ[qpos[k]].res;
         }
         if (tid == 0) s_qn = 0;
       }
       if (act) {
 #pragma unroll
         for (int k = 0; k < D1; ++k)
-          if (idx[k] < nvp) T[k] = sT[idx[k]];
+          if ((shared_k >> k) & 1u) T[k] = sT[idx[k]];
       }
       __syncthreads();
     }
@@ -1346,7 +1354,10 @@ __device__ __forceinline__ void update_patches(const DevMesh& m, const DevState&
     __syncthreads();
     for (int i = threadIdx.x; i < nvp; i += blockDim.x) {
       const int v = vs + i;
-      const int a = m.vslot_off[v], b = m.vslot_off[v + 1];
+      const int a = m.vslot_off[v];
+      // with the reference's slot limit (m.capped set) the advection sums
+      // run over the first slot_cap slots only, as the reference's update
+      const int b = (m.capped && !curvature) ? min(m.vslot_off[v + 1], a + m.slot_cap) : m.vslot_off[v + 1];
       const float oldT = sPhi[i];
       float res = oldT;
       if (!curvature) {
@@ -1645,17 +1656,21 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
     if (xd) { if (pr) LS_FIM(4, T, true, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, true, B, false); } \
     else { if (pr) LS_FIM(4, T, false, (T == 384 ? 2 : 1), true); else LS_FIM(4, T, false, B, false); } \
   } while (0)
-  if (kLbSkip && m.dim == 3 && pr) {
+  // meshes with corners beyond the reference's slot limit (reference
+  // semantics only) take the one-copy-per-thread kernel, which keeps those
+  // corners private
+  const bool compact = kLbSkip && m.dim == 3 && !m.capped;
+  if (compact && pr) {
     // fast build, tetrahedra, precision form: compacted solves, FP64 repeats
     // run densely after each sweep's FP32 pass
     const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
     if (L.fim_block <= 384) k_fim_compact<384, 2, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     else if (L.fim_block <= 512) k_fim_compact<512, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     else k_fim_compact<1024, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
-  } else if (kLbSkip && m.dim == 3 && L.pair_block > 0) {
+  } else if (compact && L.pair_block > 0) {
     // fast build, tetrahedra: compacted solves, two copies per thread
     k_fim_pair<5><<<L.fim_grid, L.pair_block, pair_smem(sp, sp.lep), st>>>(m, s, sp, cur, c);
-  } else if (kLbSkip && m.dim == 3) {
+  } else if (compact) {
     // fast build, tetrahedra: compacted solves
     const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
     if (L.fim_block <= 384) {
@@ -1733,7 +1748,7 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   L.fim_smem = (int)sizeof(float) * (2 * sp.lvp + sp.lgp);
   int occ = 0;
   L.pair_block = 0;
-  if (kLbSkip && m.dim == 3) {
+  if (kLbSkip && m.dim == 3 && !m.capped) {
     // compacted kernel (fast build): opt in to its shared memory, size the
     // grid by its occupancy
     const int maxt = L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024;

@@ -202,6 +202,16 @@ std::string build_layout(int dim, int nv, const float* xyz, int ne, const int* e
         if (p == vpart[v]) L.vslot[f[v]++] = (uint16_t)((c - L.ele_offsets[p]) * 4 + k);
       }
     if (L.lep * 4 > 0xffff) return "patch has too many element copies";
+    // corners beyond the reference's per-vertex slot limit
+    const int cap = ref_slot_cap(dim);
+    L.slot_capped.assign(full, 0);
+    L.any_capped = false;
+    for (int v = 0; v < nv; ++v)
+      for (int q = L.vslot_off[v] + cap; q < L.vslot_off[v + 1]; ++q) {
+        const int sl = L.vslot[q];
+        L.slot_capped[L.ele_offsets[vpart[v]] + (sl >> 2)] |= (uint8_t)(1u << (sl & 3));
+        L.any_capped = true;
+      }
   }
   // patch adjacency: every copy of p holds a vertex of p, so the patches of
   // its other vertices are exactly those joined to p by a mesh edge
@@ -248,6 +258,7 @@ std::string merge_layouts(const std::vector<const Layout*>& parts, Layout& out) 
   out.vslot_off.reserve(nv + 1);
   out.ele_permute.reserve(full); out.conn.reserve(full * d1); out.conn_local.reserve(full * 4);
   out.ghost_ids.reserve(ng); out.vslot.reserve(ns); out.padj.reserve(na);
+  out.slot_capped.reserve(full);
   out.xyz_p.assign((size_t)nv * 3, 0.f);
   out.patch_mesh.reserve(np);
   out.vert_offsets.push_back(0); out.ele_offsets.push_back(0); out.ghost_offsets.push_back(0);
@@ -273,6 +284,8 @@ std::string merge_layouts(const std::vector<const Layout*>& parts, Layout& out) 
     out.conn_local.insert(out.conn_local.end(), P.conn_local.begin(), P.conn_local.end());
     for (int g : P.ghost_ids) out.ghost_ids.push_back(vb + g);
     out.vslot.insert(out.vslot.end(), P.vslot.begin(), P.vslot.end());
+    out.slot_capped.insert(out.slot_capped.end(), P.slot_capped.begin(), P.slot_capped.end());
+    out.any_capped = out.any_capped || P.any_capped;
     for (int q : P.padj) out.padj.push_back(pb + q);
     out.lep = std::max(out.lep, P.lep);
     out.lvp = std::max(out.lvp, P.lvp);

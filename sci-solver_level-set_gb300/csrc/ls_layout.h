@@ -12,6 +12,9 @@
 
 namespace lsgb {
 
+// Per-vertex slots the reference's patch kernels keep (3D 32, 2D 16).
+inline int ref_slot_cap(int dim) { return dim == 3 ? 32 : 16; }
+
 struct Layout {
   int dim = 3;          // 2 = triangles, 3 = tetrahedra
   int nv = 0, ne = 0;   // vertices, elements
@@ -38,6 +41,14 @@ struct Layout {
   // slots (c - es)*4 + k of copies c of its own patch, ordered by k then c
   std::vector<int> vslot_off;
   std::vector<uint16_t> vslot;
+  // per copy: bit k set when corner k's slot comes after the first
+  // ref_slot_cap(dim) slots of its vertex.  The reference's patch kernels
+  // keep only that many slots per vertex (the fixed l_mem array of
+  // redistance_kernels3d.h:303-338 and meshFIM_kernels.h:71-105; 16 in 2D):
+  // a capped corner neither enters its vertex's minimum or sums nor receives
+  // the vertex value.  any_capped: some corner is capped.
+  std::vector<uint8_t> slot_capped;
+  bool any_capped = false;
   // patch adjacency (proper CSR, sorted neighbour lists)
   std::vector<int> padj_off, padj;
   bool has_internal_edge = false;

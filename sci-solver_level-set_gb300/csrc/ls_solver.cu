@@ -210,6 +210,9 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(upload(A, &m_.xyz, L.xyz_p, stream_), "upload");
   LS_TRY(upload(A, &m_.ipermute, ipermute, stream_), "upload");
   LS_TRY(upload(A, &m_.patch_bytes, pbytes, stream_), "upload");
+  m_.capped = nullptr;
+  m_.slot_cap = ref_slot_cap(L.dim);
+  if (ref && L.any_capped) LS_TRY(upload(A, &m_.capped, L.slot_capped, stream_), "upload");
   m_.patch_mesh = nullptr;
   m_.mesh_par = nullptr;
   if (batch) {

@@ -20,7 +20,11 @@ reference's own test meshes, through the C ABI against the CPU oracle.
     (src/LevelSet.cu:187-233) and the default parameters, graph-partitioned
     into 16-vertex patches as the reference's METIS path (the pyramid into
     3-vertex patches): the bit-exact
-    build equals the oracle bit for bit over 3 steps, in both modes.
+    build equals the oracle bit for bit over 3 steps, in both modes;
+  * the reference's own time step, meshFIM3d::GenerateData compiled from its
+    sources with its kernels run on the CPU (committed phi histories,
+    tests/golden/ref_steps.npz): the bit-exact build in the reference's
+    semantics equals it bit for bit at every step.
 """
 import numpy as np
 import pytest
@@ -29,6 +33,7 @@ import lsgb300
 import lsoracle
 import ref_fixtures
 import synth
+from test_oracle_golden import _step_cases, load_step_case
 
 pytestmark = pytest.mark.gpu
 
@@ -153,3 +158,21 @@ def test_reference_meshes_step_like_oracle(name, ref_compat):
     st = ls.stats()
     for k in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
         assert st[k] == ost[k], k
+
+
+@pytest.mark.parametrize("case", _step_cases())
+def test_bitexact_build_equals_reference_time_steps(case):
+    g = load_step_case(case)
+    hist = g["history"]
+    nsteps = len(hist) - 1
+    p = lsgb300.default_params(time_step=float(g["dt"]), bandwidth=float(g["bandwidth"]),
+                               update_kind=lsgb300.UPDATE_ADVECT, flags=lsgb300.BITEXACT | lsgb300.REF_COMPAT)
+    ls = lsgb300.LevelSet(False, p)
+    ls.set_mesh(g["xyz"], g["elems"])
+    ls.set_partition(g["npart"], int(g["nparts"]))
+    ls.set_phi(g["phi0"])
+    ls.set_velocity(g["vel"])
+    ls.setup()
+    mine, done = ls.solve(nsteps)
+    assert done == nsteps
+    assert np.array_equal(mine.view(np.uint32), hist.view(np.uint32))

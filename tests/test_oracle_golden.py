@@ -1,9 +1,12 @@
 """The oracle and the product are pinned to the reference: the oracle's local
-solvers and host curvature update reproduce the reference's own code, and the
+solvers and host curvature update reproduce the reference's own code; the
 product's patch layout builder and the oracle's restatement of it reproduce
 the layout the reference's own InitPatches / InitPatches2 /
-GenerateBlockNeighbors build (compiled from the reference sources into
-oracle/_ref; outputs committed in tests/golden/)."""
+GenerateBlockNeighbors build; and the oracle's time step reproduces the
+reference's own meshFIM3d::GenerateData (seed search, FIM redistance with its
+host-driven lists, narrowband, advection update) bit for bit.  The reference
+pieces are compiled from its sources into oracle/_ref (its kernels run on the
+CPU); their outputs are committed in tests/golden/."""
 import hashlib
 import os
 
@@ -104,3 +107,27 @@ def test_layout_equals_reference_layout(case):
     for a in lsgb300.REF_ARRAYS:
         assert _same(g, a, ls.layout(a).ravel()), (case, "product", a)
         assert _same(g, a, ol.array(a).ravel()), (case, "oracle", a)
+
+
+def _step_cases():
+    with np.load(os.path.join(GOLD, "ref_steps.npz")) as g:
+        return [str(c) for c in g["cases"]]
+
+
+def load_step_case(case):
+    """Inputs and phi history of one case of the reference's time steps."""
+    with np.load(os.path.join(GOLD, "ref_steps.npz")) as z:
+        return {k.split(":", 1)[1]: z[k] for k in z.files if k.startswith(case + ":")}
+
+
+@pytest.mark.parametrize("case", _step_cases())
+def test_oracle_equals_reference_time_steps(case):
+    g = load_step_case(case)
+    hist = g["history"]
+    nsteps = len(hist) - 1
+    ol = lsoracle.OracleLayout(3, g["xyz"], g["elems"], g["npart"], int(g["nparts"]))
+    p = ol.params(update_kind=lsoracle.UPDATE["advect"], dt=float(g["dt"]), bandwidth=float(g["bandwidth"]),
+                  curv_coeff=1.0, ref_compat=1)
+    ref, _, _, ost = ol.solve(p, g["phi0"], g["vel"], nsteps)
+    assert ost["steps_run"] == nsteps
+    assert np.array_equal(ref.view(np.uint32), hist.view(np.uint32))
