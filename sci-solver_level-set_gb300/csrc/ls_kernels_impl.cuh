@@ -1280,6 +1280,10 @@ __device__ __forceinline__ void update_copy(const DevMesh& m, const StepParams& 
         beta += Km[i];
       }
       beta = 1.0f / beta;
+      // the weights stay 0 for an element the gate drops, and the products
+      // below are formed in every case, as in the reference
+      // (meshFIM2d_kernels.h:198-236): a non-finite H then reaches the sums
+      float at[3] = {0.f, 0.f, 0.f};
       if ((double)fabsf(H) > 1e-8) {
         float alpha[3], theta = 0.f;
 #pragma unroll
@@ -1289,11 +1293,12 @@ __device__ __forceinline__ void update_copy(const DevMesh& m, const StepParams& 
           theta += fmaxf(0.f, alpha[i]);
         }
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float a = fmaxf(alpha[i], 0.f) / theta;
-          o.aH[i] = a * H;
-          o.aV[i] = a * volume;
-        }
+        for (int i = 0; i < 3; ++i) at[i] = fmaxf(alpha[i], 0.f) / theta;
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        o.aH[i] = at[i] * H;
+        o.aV[i] = at[i] * volume;
       }
     } else if (absg > 0.f) {
       o.vol = volume;
