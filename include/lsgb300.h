@@ -75,7 +75,15 @@ enum {
   LS_BITEXACT = 1u << 4,
   /* ls_step_host: stage host arrays through pinned buffers even where the
    * GPU can access pageable host memory directly (the default there). */
-  LS_HOST_STAGING = 1u << 5
+  LS_HOST_STAGING = 1u << 5,
+  /* Run every FIM iteration of a time step in one cooperative (all CTAs
+   * resident) launch, the sweep, schedule and check passes separated by
+   * grid-wide barriers, instead of three launches per iteration.  Same
+   * results.  Applies where the step's sweep kernel has a persistent form
+   * (the two-copies-per-thread tet sweep; the one-copy sweep of up to 384
+   * threads); elsewhere it is ignored.  A barrier wait that exceeds
+   * barrier_wait_limit polls abandons the step with LS_DEVICE_TIMEOUT. */
+  LS_PERSISTENT = 1u << 6
 };
 
 typedef struct ls_params {
@@ -106,6 +114,9 @@ typedef struct ls_params {
   int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 with one element copy
                              per thread; 5: two copies per thread (fast build, tetrahedra; others run 3)
                              (0 -> 5) */
+  int barrier_wait_limit; /* LS_PERSISTENT: polls (about 0.25 us apart) one grid-barrier wait may take
+                             before the step is abandoned with LS_DEVICE_TIMEOUT (0 -> 4194304, about a
+                             second) */
 } ls_params;
 
 typedef struct ls_stats {

@@ -75,11 +75,15 @@ struct DevState {
   int* counts;      // [0] list0, [1] list1, [2] newlist, [3] nblist, [4] fim iters (step)
   unsigned long long* stats;  // [0] visits [1] checks [2] nb verts [3] nb patch verts [4] nb patches [5] fim iters [6] flagged copies solved [7] FIM slab bytes [8] visits run by checks
   int* ctl;         // step control: [0] FIM loop bodies run this step, [1] iteration cap hit,
-                    // [2] previous narrowband valid (seed search restricted to it)
+                    // [2] previous narrowband valid (seed search restricted to it), [3] a grid
+                    // barrier wait of the persistent FIM kernel timed out (the launch was abandoned)
   int* sched;       // dynamic patch assignment of the sweep kernels: [0] next list entry of a
                     // sweep, [1] of a check; zero between launches (the launch's last draw
                     // resets it)
+  unsigned* gbar;   // persistent FIM kernel (kGridBarrierWords, zeroed per launch): [0] grid-barrier
+                    // arrivals since the launch started, [2 + smid] CTAs on SM smid
 };
+constexpr int kGridBarrierWords = 2 + 1024;
 
 // Learned warm start / training-pair collection buffers (null when off).
 struct DevLearn {
@@ -107,6 +111,8 @@ struct StepParams {
   int ref_compat;
   int update_kind; // 0 advect, 1 curvature
   int lvp, lgp, lep;
+  int max_fim_iters;  // persistent FIM kernel: iteration cap of one step
+  int spin_limit;     // persistent FIM kernel: polls of one grid-barrier wait before it gives up
 };
 
 __device__ __forceinline__ PatchPar patch_par(const DevMesh& m, const StepParams& sp, int p) {

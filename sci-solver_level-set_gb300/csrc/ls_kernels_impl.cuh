@@ -235,8 +235,11 @@ __device__ __forceinline__ void copy_metric(const DevMesh& m, long long c, float
 // differently contracted FMAs could make the check report a drop of more
 // than the tolerance that the following visit never applies, and two
 // patches could re-activate each other without end.
-template <int D1, int MAXT, bool XDIV, int MINB, bool PREC>
-__global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+// vb: the CTA's index in the patch assignment (blockIdx.x, or the spread
+// index of the persistent kernel)
+template <int D1, bool XDIV, bool PREC>
+__device__ __forceinline__ void fim_copy_pass(const DevMesh& m, const DevState& s, const StepParams& sp, int cur,
+                                              int check, int vb) {
   const bool CHECK = check != 0;
   extern __shared__ float smem[];
   float* sT = smem;                       // owned + ghost values
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
-  for (int li = blockIdx.x; li < count; li += gridDim.x) {
+  for (int li = vb; li < count; li += gridDim.x) {
     const int p = list[li] & ~kPrevisited;  // re-visiting is harmless: same inputs, same results
     const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
     const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
@@ -400,6 +403,11 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepP
     }
     __syncthreads();
   }
+}
+
+template <int D1, int MAXT, bool XDIV, int MINB, bool PREC>
+__global__ void __launch_bounds__(MAXT, MINB) k_fim(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+  fim_copy_pass<D1, XDIV, PREC>(m, s, sp, cur, check, blockIdx.x);
 }
 
 // Patch assignment of the sweep kernels: CTA b takes list entry b first
@@ -707,8 +715,8 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
 // that finds its patch unconverged goes on to run that patch's visit (the
 // next iteration's visit would read the same DT) and marks the patch's entry
 // in the next list with kPrevisited; the next sweep skips marked entries.
-template <int MINB>
-__global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+__device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& s, const StepParams& sp, int cur,
+                                              int check, int vb) {
   const bool CHECK = check != 0;
   extern __shared__ float4 smem4[];
   float* sT = reinterpret_cast<float*>(smem4);  // owned + ghost values
@@ -754,7 +762,7 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   const bool seed_mask = sp.lvp <= 32 * kSeedMaskWords;
   if (tid == 0) {
     s_n[0] = s_n[1] = 0;
-    s_li = blockIdx.x;
+    s_li = vb;
   }
   __syncthreads();
   for (int li = s_li; li < count;) {
@@ -1019,15 +1027,21 @@ __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, S
   }
 }
 
+template <int MINB>
+__global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+  fim_pair_pass(m, s, sp, cur, check, blockIdx.x);
+}
+
 // Schedule of one FIM iteration: one warp per patch of the current list.
-__global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
+__device__ __forceinline__ void schedule_pass(const DevMesh& m, const DevState& s, const StepParams& sp, int cur,
+                                              int vb) {
   const int count = s.counts[cur];
   const int* list = cur ? s.list1 : s.list0;
   int* nlist = cur ? s.list0 : s.list1;
   const int nxt = cur ^ 1;
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int w = warp_id_global(); w < count; w += nwarps) {
+  for (int w = (vb * blockDim.x + threadIdx.x) >> 5; w < count; w += nwarps) {
     const int p = list[w] & ~kPrevisited;
     const int vs = m.vert_off[p], ve = m.vert_off[p + 1];
     for (int v = vs + lane; v < ve; v += 32)
@@ -1059,6 +1073,152 @@ __global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
       }
     }
   }
+}
+
+__global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
+  schedule_pass(m, s, sp, cur, blockIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent FIM loop: every iteration of a step's redistance in one
+// cooperative launch (all CTAs resident), the sweep, schedule and check
+// passes separated by grid-wide barriers instead of kernel boundaries.  The
+// passes are the launch-per-pass kernels' bodies, so a step gives the same
+// bits either way (the reference's host loop this replaces:
+// redistance3d.cu:85-224).
+//
+// Grid barrier: one counter that grows by gridDim.x per barrier (reset
+// before each launch).  Thread 0 of each CTA counts the barriers it has
+// reached (epoch), adds its arrival with a release reduction and polls the
+// counter with acquire loads until it reaches epoch x gridDim.x, so the last
+// arrival releases every CTA without a reset or a second word on the
+// critical path.  Every wait is bounded: after sp.spin_limit polls the CTA
+// raises the abort word (ctl[3]) and leaves; a CTA that finds the word
+// raised, while waiting or after a barrier, leaves too, so an abort ends the
+// whole launch, and the host reports LS_DEVICE_TIMEOUT.  The acq_rel fences
+// on both sides make the passes' global writes (plain stores of every
+// thread, ordered before thread 0 by the CTA barrier) visible to the next
+// pass, which reads them with plain loads: DT, DT_out, lists, counters,
+// labels.
+__device__ __forceinline__ bool grid_sync(const DevState& s, const StepParams& sp, unsigned& epoch) {
+  __shared__ int s_go;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile int* abort_word = s.ctl + 3;
+    int go = 1;
+    epoch += 1;
+    const unsigned target = epoch * gridDim.x;
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(s.gbar) : "memory");
+    unsigned polls = 0;
+    while (true) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(s.gbar) : "memory");
+      if ((int)(v - target) >= 0) break;
+      if (*abort_word) {
+        go = 0;
+        break;
+      }
+      if (++polls > (unsigned)sp.spin_limit) {
+        atomicExch(s.ctl + 3, 1);
+        go = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    if (*abort_word) go = 0;
+    s_go = go;
+  }
+  __syncthreads();
+  return s_go != 0;
+}
+
+// The loop: iteration i sweeps list (i & 1) while it is not empty, at most
+// sp.max_fim_iters iterations (the cap sets ctl[1]).
+//
+// A cooperative launch places consecutive CTAs on the same SM (CTAs 0-19 of
+// a 760-CTA grid on four SMs, measured), while an ordinary launch spreads
+// them over the SMs; the passes give list entry b to CTA b first, so a short
+// list would run on a few SMs.  Each CTA therefore takes a spread index:
+// slot on its SM x number of SMs + rank of its SM (every SM holds the same
+// number of CTAs of a full cooperative grid; otherwise the index stays
+// blockIdx.x).  gbar[2 + smid] counts the CTAs of each SM (reset per launch).
+__device__ __forceinline__ int spread_index(const DevState& s, const StepParams& sp, unsigned& epoch, bool* ok) {
+  __shared__ int s_vb;
+  __shared__ unsigned s_slot, s_smid;
+  if (threadIdx.x == 0) {
+    unsigned smid, nsmid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
+    s_smid = smid;
+    s_slot = smid < (unsigned)(kGridBarrierWords - 2) && nsmid <= (unsigned)(kGridBarrierWords - 2)
+                 ? atomicAdd(s.gbar + 2 + smid, 1u)
+                 : 0xffffffffu;
+  }
+  *ok = grid_sync(s, sp, epoch);
+  if (!*ok) return blockIdx.x;
+  if (threadIdx.x < 32) {
+    // warp 0: SMs holding CTAs, this SM's rank among them, equal counts?
+    unsigned nsmid;
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
+    const unsigned smid = s_smid;
+    unsigned active = 0, rank = 0, per = 0;
+    bool uniform = s_slot != 0xffffffffu && nsmid <= (unsigned)(kGridBarrierWords - 2);
+    for (unsigned i0 = 0; uniform && i0 < nsmid; i0 += 32) {
+      const unsigned i = i0 + threadIdx.x;
+      const unsigned c = i < nsmid ? *reinterpret_cast<volatile unsigned*>(s.gbar + 2 + i) : 0u;
+      const unsigned has = __ballot_sync(0xffffffffu, c != 0u);
+      active += __popc(has);
+      if (smid >= i0) rank += __popc(smid - i0 >= 32 ? has : (has & ((1u << (smid - i0)) - 1u)));
+      const unsigned cmax = __reduce_max_sync(0xffffffffu, c);
+      const unsigned cmin = __reduce_min_sync(0xffffffffu, c != 0u ? c : 0xffffffffu);
+      if (has) {
+        if (per == 0) per = cmax;
+        if (cmax != per || cmin != per) uniform = false;
+      }
+    }
+    if (threadIdx.x == 0)
+      s_vb = (uniform && active * per == gridDim.x) ? (int)(s_slot * active + rank) : (int)blockIdx.x;
+  }
+  __syncthreads();
+  return s_vb;
+}
+
+template <class Pass>
+__device__ __forceinline__ void fim_loop_persistent(const DevMesh& m, const DevState& s, const StepParams& sp,
+                                                    Pass&& pass) {
+  int cur = 0;
+  unsigned epoch = 0;  // barriers passed (thread 0)
+  bool ok = true;
+  const int vb = spread_index(s, sp, epoch, &ok);
+  if (!ok) return;
+  for (int it = 0;; ++it) {
+    const int count = *reinterpret_cast<volatile int*>(s.counts + cur);
+    if (count == 0) break;
+    if (it >= sp.max_fim_iters) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) s.ctl[1] = 1;
+      break;
+    }
+    pass(cur, 0, vb);
+    if (!grid_sync(s, sp, epoch)) return;
+    schedule_pass(m, s, sp, cur, vb);
+    if (!grid_sync(s, sp, epoch)) return;
+    pass(cur, 1, vb);
+    if (!grid_sync(s, sp, epoch)) return;
+    cur ^= 1;
+  }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(192, MINB) k_fim_pair_persist(DevMesh m, DevState s, StepParams sp) {
+  fim_loop_persistent(m, s, sp, [&](int cur, int check, int vb) { fim_pair_pass(m, s, sp, cur, check, vb); });
+}
+
+template <int D1, int MAXT, bool XDIV, int MINB, bool PREC>
+__global__ void __launch_bounds__(MAXT, MINB) k_fim_persist(DevMesh m, DevState s, StepParams sp) {
+  fim_loop_persistent(m, s, sp,
+                      [&](int cur, int check, int vb) { fim_copy_pass<D1, XDIV, PREC>(m, s, sp, cur, check, vb); });
 }
 
 // Narrowband (K14) fused with the sign recovery (K10b) and the vertex-update
@@ -1707,6 +1867,76 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
   return cudaGetLastError();
 }
 
+// The persistent form of the sweep kernel launch_sweep would pick, where it
+// has one: the two-copies-per-thread kernel, or the one-copy kernel with
+// 384-thread blocks (bit-exact build, triangles, meshes with capped slots).
+// Cooperative launch: the runtime refuses a grid that cannot be resident.
+cudaError_t launch_fim_persistent(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                                  cudaStream_t st) {
+  if (L.persist_grid <= 0) return cudaErrorNotSupported;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.gridDim = dim3((unsigned)L.persist_grid);
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const bool xd = sp.xdiv != 0;
+  const bool pr = sp.tau > 0.f;
+  const bool compact = kLbSkip && m.dim == 3 && !m.capped;
+  if (compact && !pr && L.pair_block > 0) {
+    cfg.blockDim = dim3((unsigned)L.pair_block);
+    cfg.dynamicSmemBytes = (size_t)pair_smem(sp, sp.lep);
+    return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5>, m, s, sp);
+  }
+  if (compact || L.fim_block > 384) return cudaErrorNotSupported;
+  cfg.blockDim = dim3((unsigned)L.fim_block);
+  const int psmem = L.fim_smem + (int)sizeof(DeferredSolve) * kDeferCap;
+  cfg.dynamicSmemBytes = (size_t)(pr ? psmem : L.fim_smem);
+  if (m.dim == 3) {
+    if (pr) {
+      if (xd) return cudaLaunchKernelEx(&cfg, k_fim_persist<4, 384, true, 2, true>, m, s, sp);
+      return cudaLaunchKernelEx(&cfg, k_fim_persist<4, 384, false, 2, true>, m, s, sp);
+    }
+    if (xd) return cudaLaunchKernelEx(&cfg, k_fim_persist<4, 384, true, 2, false>, m, s, sp);
+    return cudaLaunchKernelEx(&cfg, k_fim_persist<4, 384, false, 2, false>, m, s, sp);
+  }
+  return cudaLaunchKernelEx(&cfg, k_fim_persist<3, 384, false, 2, false>, m, s, sp);
+}
+
+// Resident CTAs of the persistent kernel launch_fim_persistent picks (0
+// where there is no persistent form).
+cudaError_t configure_persistent(const DevMesh& m, const StepParams& sp, Launch& L) {
+  L.persist_grid = 0;
+  const bool xd = sp.xdiv != 0;
+  const bool pr = sp.tau > 0.f;
+  const bool compact = kLbSkip && m.dim == 3 && !m.capped;
+  int occ = 0;
+  cudaError_t e = cudaSuccess;
+  auto query = [&](const void* fn, int block, int smem) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, smem);
+  };
+  if (compact && !pr && L.pair_block > 0) {
+    query((const void*)k_fim_pair_persist<5>, L.pair_block, pair_smem(sp, sp.lep));
+  } else if (!compact && L.fim_block <= 384) {
+    const int psmem = L.fim_smem + (int)sizeof(DeferredSolve) * kDeferCap;
+    const int sm = pr ? psmem : L.fim_smem;
+    const void* fn = m.dim == 3 ? (pr ? (xd ? (const void*)k_fim_persist<4, 384, true, 2, true>
+                                           : (const void*)k_fim_persist<4, 384, false, 2, true>)
+                                      : (xd ? (const void*)k_fim_persist<4, 384, true, 2, false>
+                                            : (const void*)k_fim_persist<4, 384, false, 2, false>))
+                                : (const void*)k_fim_persist<3, 384, false, 2, false>;
+    query(fn, L.fim_block, sm);
+  } else {
+    return cudaSuccess;
+  }
+  if (e != cudaSuccess) return e;
+  L.persist_grid = occ > 0 ? L.sms * occ : 0;
+  return cudaSuccess;
+}
+
 cudaError_t launch_schedule(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, const Launch& L,
                             cudaStream_t st) {
   k_schedule<<<L.warp_grid, 256, 0, st>>>(m, s, sp, cur);
@@ -1830,12 +2060,13 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
   L.upd_grid = L.sms * occ;
   L.warp_grid = L.sms * 8;
   L.flat_grid = L.sms * 8;
-  return cudaSuccess;
+  return configure_persistent(m, sp, L);
 }
 
 
 const KernelSet& kernel_table() {
-  static const KernelSet t = {configure_launch, launch_reset, launch_seed,    launch_sweep, launch_schedule,
-                              launch_narrowband, launch_update, launch_unpermute, launch_permute, launch_learn};
+  static const KernelSet t = {configure_launch,  launch_reset,  launch_seed,      launch_sweep,
+                              launch_schedule,   launch_fim_persistent, launch_narrowband, launch_update,
+                              launch_unpermute,  launch_permute, launch_learn};
   return t;
 }

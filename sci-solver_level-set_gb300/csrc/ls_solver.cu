@@ -241,6 +241,8 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(dalloc(A, &s_.stats, 9), "alloc");
   LS_TRY(dalloc(A, &s_.ctl, 4), "alloc");
   LS_TRY(dalloc(A, &s_.sched, 4), "alloc");
+  LS_TRY(dalloc(A, &s_.gbar, kGridBarrierWords), "alloc");
+  LS_TRY(cudaMemsetAsync(s_.gbar, 0, sizeof(unsigned) * kGridBarrierWords, stream_), "memset");
   LS_TRY(dalloc(A, &d_tmp_, nv), "alloc");
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 8, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.stats, 0, sizeof(unsigned long long) * 9, stream_), "memset");
@@ -269,8 +271,12 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   sp_.lvp = L.lvp;
   sp_.lgp = L.lgp;
   sp_.lep = L.lep;
+  sp_.max_fim_iters = cfg.max_fim_iters;
+  sp_.spin_limit = cfg.spin_limit > 0 ? cfg.spin_limit : (1 << 22);
   (void)d1;
   LS_TRY(K_->configure(m_, sp_, L_), "configure");
+  // the persistent FIM loop where the chosen sweep kernel has that form
+  persistent_ = cfg_.persistent && L_.persist_grid > 0;
   if (cfg_.graph_chunk < 2) cfg_.graph_chunk = 2;
   if (cfg_.graph_chunk & 1) cfg_.graph_chunk++;
   if (cfg_.use_graph) {
@@ -305,7 +311,63 @@ __global__ void k_step_tail(const int* counts, int* ctl) {
 // bodies of graph_chunk iterations until the active list drains (or the
 // iteration cap), then narrowband and update.  The host launches it and
 // reads the counters once per step.
+// The persistent form: the whole step is one captured sequence (seed part,
+// the cooperative FIM launch, narrowband and update), no conditional node.
+// Returns false when the runtime will not capture the cooperative launch (the
+// step then launches kernel by kernel).
+bool Solver::build_persistent_graph(std::string* err) {
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+  cudaError_t e = step_persistent_launches(-1);
+  cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();  // clear the capture failure
+    return false;
+  }
+  cudaError_t e3 = cudaGraphInstantiate(&graph_exec_, g, 0);
+  graph_ = g;
+  if (e3 != cudaSuccess) {
+    *err = std::string("graph instantiate: ") + cudaGetErrorString(e3);
+    graph_exec_ = nullptr;
+    return false;
+  }
+  return true;
+}
+
+// One step of the persistent form, launch by launch (use_all < 0: the seed
+// kernel decides from the step-control flag, as in a graph).
+cudaError_t Solver::step_persistent_launches(int use_all) {
+  cudaError_t err = cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.ctl, 0, sizeof(int) * 2, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.ctl + 3, 0, sizeof(int), stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.gbar, 0, sizeof(unsigned) * kGridBarrierWords, stream_);
+  // the patch-draw counters are zero after every complete launch; a launch
+  // abandoned on a barrier timeout can leave them set
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.sched, 0, sizeof(int) * 2, stream_);
+  if (err == cudaSuccess) err = K_->reset(m_, s_, sp_, L_, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_);
+  if (err == cudaSuccess) err = K_->seed(m_, s_, use_all, sp_.scale, L_, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.counts + 3, 0, sizeof(int), stream_);
+  if (err == cudaSuccess) err = K_->fim_persistent(m_, s_, sp_, L_, stream_);
+  if (err == cudaSuccess) err = K_->narrowband(m_, s_, sp_, L_, stream_);
+  if (err == cudaSuccess) {
+    k_step_tail<<<1, 32, 0, stream_>>>(s_.counts, s_.ctl);
+    err = cudaGetLastError();
+  }
+  if (cfg_.update_kind != 2)
+    for (int it = 0; it < cfg_.inside_niter && err == cudaSuccess; ++it) err = K_->update(m_, s_, sp_, L_, stream_);
+  return err;
+}
+
 std::string Solver::build_graph() {
+  if (persistent_) {
+    std::string err;
+    if (build_persistent_graph(&err)) return "";
+    if (!err.empty()) return err;
+    return "";  // no graph: the persistent step launches kernel by kernel
+  }
   const int chunk = cfg_.graph_chunk;
   const int max_bodies = (cfg_.max_fim_iters + chunk - 1) / chunk;
   cudaGraph_t pre = nullptr, post = nullptr;
@@ -423,8 +485,13 @@ std::string Solver::one_step(bool* empty_nb) {
     LS_TRY(cudaMemcpyAsync(h_counts_ + 8, s_.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream_), "d2h");
     LS_TRY(cudaStreamSynchronize(stream_), "step sync");
     const int bodies = h_counts_[8];
-    st_.kernel_launches += 5LL + (3LL * cfg_.graph_chunk + 1) * bodies +
-                           (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0);
+    st_.kernel_launches += persistent_ ? 5LL + (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0)
+                                       : 5LL + (3LL * cfg_.graph_chunk + 1) * bodies +
+                                             (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0);
+    if (h_counts_[11]) {
+      status_ = 3;
+      return "a grid barrier wait of the persistent FIM kernel timed out";
+    }
     if (h_counts_[9]) {
       status_ = 3;
       return "FIM did not converge within max_fim_iters iterations";
@@ -434,6 +501,35 @@ std::string Solver::one_step(bool* empty_nb) {
     return "";
   }
   const int use_all = have_nb_ ? 0 : 1;
+  if (persistent_) {
+    // the persistent step launch by launch (profiled: the FIM loop kernel's
+    // time is recorded as the sweep time)
+    ProfEvent pe{};
+    if (cfg_.profile) {
+      LS_TRY(prof_begin(pe, 0), "event");
+      LS_TRY(cudaEventRecord(pe.a, stream_), "event");
+    }
+    LS_TRY(step_persistent_launches(use_all), "persistent step");
+    if (cfg_.profile) {
+      LS_TRY(cudaEventRecord(pe.b, stream_), "event");
+      prof_.push_back(pe);
+    }
+    LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaMemcpyAsync(h_counts_ + 8, s_.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaStreamSynchronize(stream_), "step sync");
+    st_.kernel_launches += 5LL + (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0);
+    if (h_counts_[11]) {
+      status_ = 3;
+      return "a grid barrier wait of the persistent FIM kernel timed out";
+    }
+    if (h_counts_[9]) {
+      status_ = 3;
+      return "FIM did not converge within max_fim_iters iterations";
+    }
+    have_nb_ = h_counts_[3] != 0;
+    *empty_nb = !have_nb_;
+    return "";
+  }
   LS_TRY(cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_), "memset");
   LS_TRY(cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_), "memset");
   LS_TRY(K_->reset(m_, s_, sp_, L_, stream_), "reset");

@@ -16,6 +16,7 @@ struct Launch {
   int sms;
   int fim_grid, fim_block, fim_smem;
   int pair_block;  // threads of the two-copies-per-thread sweep kernel (0: not used)
+  int persist_grid;  // CTAs of the persistent FIM kernel (all resident; 0: no persistent form here)
   int upd_grid, upd_block, upd_smem;
   int seed_grid;
   int warp_grid;
@@ -33,6 +34,9 @@ struct KernelSet {
                        const Launch& L, cudaStream_t st);
   cudaError_t (*schedule)(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, const Launch& L,
                           cudaStream_t st);
+  // every FIM iteration of a step in one cooperative launch (L.persist_grid > 0)
+  cudaError_t (*fim_persistent)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
+                                cudaStream_t st);
   cudaError_t (*narrowband)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L,
                             cudaStream_t st);
   cudaError_t (*update)(const DevMesh& m, const DevState& s, const StepParams& sp, const Launch& L, cudaStream_t st);
@@ -65,6 +69,8 @@ struct SolverConfig {
   double length_scale = 0.0;
   double fp64_tau = 3.814697265625e-06;  // 2^-18
   int host_staging = 0;  // 1: host arrays go through pinned staging even where the GPU can read pageable memory
+  int persistent = 0;    // 1: a step's FIM loop runs as one cooperative launch where the kernel has that form
+  int spin_limit = 1 << 22;  // polls of one grid-barrier wait of the persistent kernel
   // batches (Layout::patch_mesh set): per-mesh dt, bandwidth, curvature
   // coefficient and FIM length scale (<= 0: the mesh's mean edge)
   std::vector<double> mesh_dt, mesh_bandwidth, mesh_curv, mesh_length_scale;
@@ -121,6 +127,9 @@ class Solver {
   std::string learn_buffers();
   std::string fim_loop(const StepParams& sp);
   std::string build_graph();
+  bool build_persistent_graph(std::string* err);
+  cudaError_t step_persistent_launches(int use_all);
+  bool persistent_ = false;        // the step's FIM loop is one cooperative launch
   void pull_stats();
   bool stats_stale_ = false;  // device counters changed since the last pull_stats
   // event pairs around the launches of profiled steps (cfg_.profile); kind 0

@@ -17,6 +17,7 @@ LS_OK, LS_BAD_INPUT, LS_PATCH_TOO_LARGE, LS_DEVICE_TIMEOUT, LS_CUDA_ERROR, LS_NO
 UPDATE_ADVECT, UPDATE_CURVATURE, UPDATE_NONE = 0, 1, 2
 REF_COMPAT, FP64_FLAGGED, PROFILE, NO_GRAPH, BITEXACT = 1, 2, 4, 8, 16
 HOST_STAGING = 1 << 5
+PERSISTENT = 1 << 6
 
 # reference-format layout arrays (ls_get_layout selectors)
 REF_ARRAYS = {
@@ -34,7 +35,7 @@ class Params(ctypes.Structure):
         ("update_kind", ctypes.c_int), ("curv_coeff", ctypes.c_double), ("flags", ctypes.c_uint),
         ("fim_sweeps", ctypes.c_int), ("max_fim_iters", ctypes.c_int), ("smallnum", ctypes.c_double),
         ("largenum", ctypes.c_double), ("length_scale", ctypes.c_double), ("fp64_threshold", ctypes.c_double),
-        ("graph_chunk", ctypes.c_int), ("fim_ctas_per_sm", ctypes.c_int),
+        ("graph_chunk", ctypes.c_int), ("fim_ctas_per_sm", ctypes.c_int), ("barrier_wait_limit", ctypes.c_int),
     ]
 
 
