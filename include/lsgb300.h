@@ -116,7 +116,9 @@ typedef struct ls_params {
                              (0 -> 5) */
   int barrier_wait_limit; /* LS_PERSISTENT: polls (about 0.25 us apart) one grid-barrier wait may take
                              before the step is abandoned with LS_DEVICE_TIMEOUT (0 -> 4194304, about a
-                             second) */
+                             second).  The FIM kernel's wait for its geometry slab copies is bounded by
+                             about a second of SM clock cycles.  Negative: every such wait gives up at
+                             its first check (a setting for testing the timeout paths) */
 } ls_params;
 
 typedef struct ls_stats {

@@ -131,7 +131,7 @@ lsgb::SolverConfig solver_config(const ls_params& p) {
   cfg.bit_exact = (p.flags & LS_BITEXACT) ? 1 : 0;
   cfg.host_staging = (p.flags & LS_HOST_STAGING) ? 1 : 0;
   cfg.persistent = (p.flags & LS_PERSISTENT) ? 1 : 0;
-  cfg.spin_limit = p.barrier_wait_limit > 0 ? p.barrier_wait_limit : (1 << 22);
+  cfg.spin_limit = p.barrier_wait_limit != 0 ? (p.barrier_wait_limit > 0 ? p.barrier_wait_limit : -1) : (1 << 22);
   cfg.niter = p.fim_sweeps;
   cfg.inside_niter = p.inside_iterations > 0 ? p.inside_iterations : 1;
   cfg.max_fim_iters = p.max_fim_iters > 0 ? p.max_fim_iters : 100000;

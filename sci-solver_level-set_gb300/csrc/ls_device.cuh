@@ -49,6 +49,14 @@ struct DevMesh {
   // coefficient}; null for a single mesh (StepParams hold them)
   const int* patch_mesh;
   const float4* mesh_par;
+  // per copy, precomputed once per mesh for the two-copies-per-thread tet
+  // sweep (null otherwise): the 11 metric terms of copy_metric as three
+  // float4 (geo_m[3c .. 3c+2], last lane 0) and the heights of A, B, C, D
+  // over their opposite faces (geo_h[c]); a patch's copies are contiguous,
+  // so its records are two contiguous slabs, staged by bulk asynchronous
+  // copies
+  const float4* geo_m;
+  const float4* geo_h;
 };
 
 // Bandwidth (FIM frame), FIM frame scale, dt and curvature coefficient of
@@ -75,8 +83,9 @@ struct DevState {
   int* counts;      // [0] list0, [1] list1, [2] newlist, [3] nblist, [4] fim iters (step)
   unsigned long long* stats;  // [0] visits [1] checks [2] nb verts [3] nb patch verts [4] nb patches [5] fim iters [6] flagged copies solved [7] FIM slab bytes [8] visits run by checks
   int* ctl;         // step control: [0] FIM loop bodies run this step, [1] iteration cap hit,
-                    // [2] previous narrowband valid (seed search restricted to it), [3] a grid
-                    // barrier wait of the persistent FIM kernel timed out (the launch was abandoned)
+                    // [2] previous narrowband valid (seed search restricted to it), [3] a wait of a
+                    // FIM kernel timed out and the launch was abandoned (1: grid barrier of the
+                    // persistent kernel, 2: geometry slab copy); cleared at every step start
   int* sched;       // dynamic patch assignment of the sweep kernels: [0] next list entry of a
                     // sweep, [1] of a check; zero between launches (the launch's last draw
                     // resets it)
@@ -112,7 +121,9 @@ struct StepParams {
   int update_kind; // 0 advect, 1 curvature
   int lvp, lgp, lep;
   int max_fim_iters;  // persistent FIM kernel: iteration cap of one step
-  int spin_limit;     // persistent FIM kernel: polls of one grid-barrier wait before it gives up
+  int spin_limit;     // polls of one grid-barrier wait of the persistent FIM kernel before it gives up;
+                      // < 0: every wait of the FIM kernels (grid barrier, geometry slab copy) gives up
+                      // at its first check (the setting that tests the timeout paths)
 };
 
 __device__ __forceinline__ PatchPar patch_par(const DevMesh& m, const StepParams& sp, int p) {

@@ -696,6 +696,83 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
   else reinterpret_cast<float*>(sR)[4 * cc + k] = nw;
 }
 
+// Per-copy geometry of the two-copies-per-thread sweep, computed once per
+// mesh: the copy's metric terms (copy_metric) as three float4 and the heights
+// of its four vertices over their opposite faces, the same expressions the
+// one-copy kernels evaluate per visit.
+__global__ void k_geometry(DevMesh m, float4* gm, float4* gh) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < m.full; c += stride) {
+    float Mt[11];
+    copy_metric<4>(m, c, Mt);
+    gm[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
+    gm[3 * c + 1] = make_float4(Mt[4], Mt[5], Mt[6], Mt[7]);
+    gm[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], 0.f);
+    const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
+    const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
+    const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
+                       ACCD * (ACBC * BCCD - BCBC * ACCD);
+    gh[c] = make_float4(sqrtf(fmaxf(det3 / (BCBC * CDCD - BCCD * BCCD), 0.f)),   // A over BCD
+                        sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f)),   // B over ACD
+                        sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f)),   // C over ABD
+                        sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f)));  // D over ABC
+  }
+}
+
+// Bulk asynchronous copies of a patch's geometry slabs into shared memory,
+// completed on a CTA mbarrier (one phase per patch, one arrival: the issuing
+// thread's, which also sets the expected bytes).  Sources are this GPU's
+// global memory, destinations this CTA's shared memory; both slabs start on
+// 16-byte boundaries and are multiples of 16 bytes long (float4 records).
+constexpr long long kSlabWaitCycles = 1ll << 31;  // about one second at the SM clock
+
+__device__ __forceinline__ unsigned smem_u32addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void slab_bar_init(unsigned bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void slab_bar_inval(unsigned bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void geo_issue(const DevMesh& m, int es, int nep, float4* sM, float4* sH, unsigned bar) {
+  const unsigned bm = 48u * (unsigned)nep, bh = 16u * (unsigned)nep;
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(bar),
+               "r"(bm + bh)
+               : "memory");
+  if (nep > 0) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32addr(sM)),
+                 "l"(__cvta_generic_to_global(m.geo_m + 3ll * es)), "r"(bm), "r"(bar)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32addr(sH)),
+                 "l"(__cvta_generic_to_global(m.geo_h + es)), "r"(bh), "r"(bar)
+                 : "memory");
+  }
+}
+
+// Bounded wait for the phase of the given parity: true once it completed,
+// false after kSlabWaitCycles (at once when give_up is set: the test setting
+// of the timeout path).
+__device__ __forceinline__ bool slab_wait(unsigned bar, unsigned parity, bool give_up) {
+  if (give_up) return false;
+  const long long t0 = clock64();
+  while (true) {
+    unsigned ok;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kSlabWaitCycles) return false;
+  }
+}
+
 // Fast-build FIM patch visit for tetrahedra, two element copies per thread.
 // The same sweep as k_fim_compact (listing with the lower bound, the
 // unchanged-input and unread-ghost skips; dense predicated solves; per-vertex
@@ -710,6 +787,13 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
 // connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k),
 // flags uchar [ncap] (changed vertices in bits 0-3, ghost vertices in bits
 // 4-7).
+// The metric and height slabs come from the per-mesh geometry records
+// (k_geometry) by two bulk asynchronous copies that thread 0 issues at the
+// start of each patch; they land while the threads gather the values and
+// load the connectivity, and thread 0 waits for them (bounded) before the
+// setup barrier.  A wait that runs out sets ctl[3] = 2, waits once more for
+// the copies in flight and ends the CTA's pass; the host then reports
+// LS_DEVICE_TIMEOUT.
 // Patches: the list entry of the CTA's index first, later ones from
 // draw_patch.  On a check launch of at least two patches per CTA, a check
 // that finds its patch unconverged goes on to run that patch's visit (the
@@ -734,6 +818,8 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   __shared__ int s_li;    // list entry of the next patch
   __shared__ int s_ng;    // ghost-target solves listed when a check becomes a visit
   __shared__ unsigned s_seed[kSeedMaskWords];  // seed flags of the owned vertices (bit i = vertex i)
+  __shared__ __align__(8) unsigned long long s_bar;  // geometry slab copies of the current patch
+  __shared__ int s_err;  // a slab wait ran out: the pass ends
   const int* list = CHECK ? s.newlist : (cur ? s.list1 : s.list0);
   const int count = CHECK ? s.counts[2] : s.counts[cur];
   const int nxt = cur ^ 1;
@@ -750,6 +836,9 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   if (CHECK && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&s.stats[1], (unsigned long long)count);
   const int niter = CHECK ? 1 : sp.niter;
   const int tid = threadIdx.x;
+  const unsigned bar = smem_u32addr(&s_bar);
+  unsigned phase = 0;      // thread 0: parity of the slab copies' current phase
+  bool in_flight = false;  // thread 0: copies whose wait ran out twice
   // first entry by CTA index, later ones drawn from a counter (draw_patch)
   int* next = s.sched + (CHECK ? 1 : 0);
   // visits run by the checks that activate them only pay when the check
@@ -763,6 +852,8 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   if (tid == 0) {
     s_n[0] = s_n[1] = 0;
     s_li = vb;
+    s_err = 0;
+    slab_bar_init(bar);
   }
   __syncthreads();
   for (int li = s_li; li < count;) {
@@ -774,6 +865,10 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       const int vs = m.vert_off[p], nvp = m.vert_off[p + 1] - vs;
       const int gs = m.ghost_off[p], ngp = m.ghost_off[p + 1] - gs;
       const int es = m.ele_off[p], nep = m.ele_off[p + 1] - es;
+      // the metric and height slabs: in flight while the values, seed flags
+      // and connectivity load (the previous patch's last reads of sM and sH
+      // came before its final barrier)
+      if (tid == 0) geo_issue(m, es, nep, sM, sH, bar);
       for (int i = tid; i < nvp + ngp; i += blockDim.x)
         sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
       // whole warps run each 32-vertex word (the block is whole warps and the
@@ -783,29 +878,15 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
           const unsigned b = __ballot_sync(0xffffffffu, i < nvp && s.seed[vs + i] != 0);
           if ((i & 31) == 0) s_seed[i >> 5] = b;
         }
-      // the copies' connectivity, metric, heights and flags do not depend on
-      // the values, so their loads overlap the value gathers above (the
-      // previous patch's last reads of these arrays came before its final
-      // barrier)
+      // the copies' connectivity and flags do not depend on the values, so
+      // their loads overlap the value gathers above (the previous patch's
+      // last reads of these arrays came before its final barrier)
   #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         if (c < nep) {
           const ushort4 cv = m.conn[es + c];
           sC[c] = cv;
-          float Mt[11];
-          copy_metric<4>(m, (long long)es + c, Mt);
-          sM[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
-          sM[3 * c + 1] = make_float4(Mt[4], Mt[5], Mt[6], Mt[7]);
-          sM[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], 0.f);
-          const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
-          const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
-          const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
-                             ACCD * (ACBC * BCCD - BCBC * ACCD);
-          sH[c] = make_float4(sqrtf(fmaxf(det3 / (BCBC * CDCD - BCCD * BCCD), 0.f)),   // A over BCD
-                              sqrtf(fmaxf(det3 / (ACAC * CDCD - ACCD * ACCD), 0.f)),   // B over ACD
-                              sqrtf(fmaxf(det3 / (ADAD * BDBD - ADBD * ADBD), 0.f)),   // C over ABD
-                              sqrtf(fmaxf(det3 / (ACAC * BCBC - ACBC * ACBC), 0.f)));  // D over ABC
           const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
                                  (cv.w >= nvp ? 8u : 0u);
           sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
@@ -814,8 +895,17 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       if (tid == 0) {
         s_min = 0x7f800000u;
         s_ng = 0;
+        if (!slab_wait(bar, phase, sp.spin_limit < 0)) {
+          // abandoned: the host reports a timeout; the copies are waited for
+          // once more so that none is in flight when the CTA leaves
+          atomicExch(s.ctl + 3, 2);
+          in_flight = !slab_wait(bar, phase, false);
+          s_err = 1;
+        }
+        phase ^= 1u;
       }
       __syncthreads();
+      if (s_err) break;
       auto is_seed = [&](int i) -> bool {
         return seed_mask ? ((s_seed[i >> 5] >> (i & 31)) & 1u) != 0u : s.seed[vs + i] != 0;
       };
@@ -1025,6 +1115,9 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       li = s_li;
     }
   }
+  // every phase was waited for (unless a copy stayed in flight after a
+  // timeout): the mbarrier can go
+  if (tid == 0 && !in_flight) slab_bar_inval(bar);
 }
 
 template <int MINB>
@@ -1092,7 +1185,8 @@ __global__ void k_schedule(DevMesh m, DevState s, StepParams sp, int cur) {
 // reached (epoch), adds its arrival with a release reduction and polls the
 // counter with acquire loads until it reaches epoch x gridDim.x, so the last
 // arrival releases every CTA without a reset or a second word on the
-// critical path.  Every wait is bounded: after sp.spin_limit polls the CTA
+// critical path.  Every wait is bounded: after sp.spin_limit polls (one if
+// it is negative) the CTA
 // raises the abort word (ctl[3]) and leaves; a CTA that finds the word
 // raised, while waiting or after a barrier, leaves too, so an abort ends the
 // whole launch, and the host reports LS_DEVICE_TIMEOUT.  The acq_rel fences
@@ -1119,7 +1213,7 @@ __device__ __forceinline__ bool grid_sync(const DevState& s, const StepParams& s
         go = 0;
         break;
       }
-      if (++polls > (unsigned)sp.spin_limit) {
+      if (++polls > (sp.spin_limit < 0 ? 0u : (unsigned)sp.spin_limit)) {
         atomicExch(s.ctl + 3, 1);
         go = 0;
         break;
@@ -1970,6 +2064,13 @@ cudaError_t launch_permute(const DevMesh& m, const float* in, float* out, const 
   return cudaGetLastError();
 }
 
+// Geometry records of the two-copies-per-thread sweep (L.pair_block > 0).
+cudaError_t launch_geometry(const DevMesh& m, float4* gm, float4* gh, const Launch& L, cudaStream_t st) {
+  if (L.pair_block <= 0 || m.full == 0) return cudaSuccess;
+  k_geometry<<<L.flat_grid, 256, 0, st>>>(m, gm, gh);
+  return cudaGetLastError();
+}
+
 cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -2067,6 +2168,6 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
 const KernelSet& kernel_table() {
   static const KernelSet t = {configure_launch,  launch_reset,  launch_seed,      launch_sweep,
                               launch_schedule,   launch_fim_persistent, launch_narrowband, launch_update,
-                              launch_unpermute,  launch_permute, launch_learn};
+                              launch_unpermute,  launch_permute, launch_learn,     launch_geometry};
   return t;
 }

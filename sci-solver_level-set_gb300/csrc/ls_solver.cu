@@ -209,12 +209,13 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   LS_TRY(upload(A, &m_.padj, L.padj, stream_), "upload");
   LS_TRY(upload(A, &m_.xyz, L.xyz_p, stream_), "upload");
   LS_TRY(upload(A, &m_.ipermute, ipermute, stream_), "upload");
-  LS_TRY(upload(A, &m_.patch_bytes, pbytes, stream_), "upload");
   m_.capped = nullptr;
   m_.slot_cap = ref_slot_cap(L.dim);
   if (ref && L.any_capped) LS_TRY(upload(A, &m_.capped, L.slot_capped, stream_), "upload");
   m_.patch_mesh = nullptr;
   m_.mesh_par = nullptr;
+  m_.geo_m = nullptr;
+  m_.geo_h = nullptr;
   if (batch) {
     std::vector<float4> mp(nmesh);
     for (int k = 0; k < nmesh; ++k)
@@ -272,9 +273,24 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   sp_.lgp = L.lgp;
   sp_.lep = L.lep;
   sp_.max_fim_iters = cfg.max_fim_iters;
-  sp_.spin_limit = cfg.spin_limit > 0 ? cfg.spin_limit : (1 << 22);
+  sp_.spin_limit = cfg.spin_limit != 0 ? cfg.spin_limit : (1 << 22);
   (void)d1;
   LS_TRY(K_->configure(m_, sp_, L_), "configure");
+  if (L_.pair_block > 0) {
+    // the two-copies-per-thread sweep stages precomputed per-copy geometry
+    // (metric terms and heights, 64 bytes a copy) instead of the 24 bytes of
+    // local coordinates it would otherwise turn into them on every visit
+    float4* geo = nullptr;
+    LS_TRY(dalloc(A, &geo, (size_t)4 * (size_t)full), "alloc");
+    m_.geo_m = geo;
+    m_.geo_h = geo + 3 * full;
+    LS_TRY(K_->geometry(m_, geo, geo + 3 * full, L_, stream_), "geometry");
+    for (int p = 0; p < np; ++p) {
+      const long long nep = L.ele_offsets[p + 1] - L.ele_offsets[p];
+      pbytes[p] += (int)(nep * (64 - 4 * nc));
+    }
+  }
+  LS_TRY(upload(A, &m_.patch_bytes, pbytes, stream_), "upload");
   // the persistent FIM loop where the chosen sweep kernel has that form
   persistent_ = cfg_.persistent && L_.persist_grid > 0;
   if (cfg_.graph_chunk < 2) cfg_.graph_chunk = 2;
@@ -295,7 +311,7 @@ namespace {
 __global__ void k_loop_cond(const int* counts, int* ctl, cudaGraphConditionalHandle h, int max_bodies) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     const int b = ++ctl[0];
-    const bool more = counts[0] > 0;
+    const bool more = counts[0] > 0 && ctl[3] == 0;  // a FIM kernel wait that ran out ends the loop
     if (more && b >= max_bodies) ctl[1] = 1;
     cudaGraphSetConditional(h, (more && b < max_bodies) ? 1u : 0u);
   }
@@ -377,6 +393,7 @@ std::string Solver::build_graph() {
   err = cudaMemsetAsync(s_.counts, 0, sizeof(int) * 3, stream_);
   if (err == cudaSuccess) err = cudaMemsetAsync(s_.counts + 4, 0, sizeof(int), stream_);
   if (err == cudaSuccess) err = cudaMemsetAsync(s_.ctl, 0, sizeof(int) * 2, stream_);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s_.ctl + 3, 0, sizeof(int), stream_);
   if (err == cudaSuccess) err = K_->reset(m_, s_, sp_, L_, stream_);
   if (err == cudaSuccess) err = cudaMemsetAsync(s_.blabel, 0, sizeof(int) * m_.nparts, stream_);
   if (err == cudaSuccess) err = K_->seed(m_, s_, -1, sp_.scale, L_, stream_);
@@ -445,6 +462,8 @@ std::string Solver::fim_loop(const StepParams& sp) {
     prof_.push_back(pe);
     return e;
   };
+  // a wait of the FIM kernels that runs out sets ctl[3] (read at every sync)
+  LS_TRY(cudaMemsetAsync(s_.ctl + 3, 0, sizeof(int), stream_), "memset");
   while (true) {
     for (int i = 0; i < cfg_.graph_chunk; ++i) {
       const int cur = i & 1;
@@ -455,7 +474,12 @@ std::string Solver::fim_loop(const StepParams& sp) {
     launched += cfg_.graph_chunk;
     st_.kernel_launches += 3LL * cfg_.graph_chunk;
     LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
+    LS_TRY(cudaMemcpyAsync(h_counts_ + 8, s_.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream_), "d2h");
     LS_TRY(cudaStreamSynchronize(stream_), "fim sync");
+    if (h_counts_[11]) {
+      status_ = 3;
+      return "a geometry slab copy wait of the FIM kernel timed out";
+    }
     if (h_counts_[0] == 0) break;
     if (launched >= cfg_.max_fim_iters) {
       status_ = 3;
@@ -490,7 +514,8 @@ std::string Solver::one_step(bool* empty_nb) {
                                              (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0);
     if (h_counts_[11]) {
       status_ = 3;
-      return "a grid barrier wait of the persistent FIM kernel timed out";
+      return h_counts_[11] == 1 ? "a grid barrier wait of the persistent FIM kernel timed out"
+                                : "a geometry slab copy wait of the FIM kernel timed out";
     }
     if (h_counts_[9]) {
       status_ = 3;
@@ -520,7 +545,8 @@ std::string Solver::one_step(bool* empty_nb) {
     st_.kernel_launches += 5LL + (cfg_.update_kind != 2 ? 2LL * cfg_.inside_niter : 0);
     if (h_counts_[11]) {
       status_ = 3;
-      return "a grid barrier wait of the persistent FIM kernel timed out";
+      return h_counts_[11] == 1 ? "a grid barrier wait of the persistent FIM kernel timed out"
+                                : "a geometry slab copy wait of the FIM kernel timed out";
     }
     if (h_counts_[9]) {
       status_ = 3;

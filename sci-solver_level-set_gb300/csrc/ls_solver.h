@@ -45,6 +45,9 @@ struct KernelSet {
   // learned warm start / collection kernels (op: LEARN_*)
   cudaError_t (*learn)(int op, const DevMesh& m, const DevState& s, const StepParams& sp, const DevLearn& lr, int arg,
                        float fa, const Launch& L, cudaStream_t st);
+  // per-copy geometry records of the two-copies-per-thread sweep (written
+  // when L.pair_block > 0; gm: 3 float4 per copy, gh: 1)
+  cudaError_t (*geometry)(const DevMesh& m, float4* gm, float4* gh, const Launch& L, cudaStream_t st);
 };
 const KernelSet& kernels_fast();
 const KernelSet& kernels_exact();
@@ -70,7 +73,8 @@ struct SolverConfig {
   double fp64_tau = 3.814697265625e-06;  // 2^-18
   int host_staging = 0;  // 1: host arrays go through pinned staging even where the GPU can read pageable memory
   int persistent = 0;    // 1: a step's FIM loop runs as one cooperative launch where the kernel has that form
-  int spin_limit = 1 << 22;  // polls of one grid-barrier wait of the persistent kernel
+  int spin_limit = 1 << 22;  // polls of one grid-barrier wait of the persistent kernel (< 0: every FIM
+                             // kernel wait gives up at its first check)
   // batches (Layout::patch_mesh set): per-mesh dt, bandwidth, curvature
   // coefficient and FIM length scale (<= 0: the mesh's mean edge)
   std::vector<double> mesh_dt, mesh_bandwidth, mesh_curv, mesh_length_scale;

@@ -297,3 +297,25 @@ def test_fim_iteration_cap_reports_timeout():
     with pytest.raises(lsgb300.LevelSetError) as e:
         ls.solve(1)
     assert e.value.code == lsgb300.LS_DEVICE_TIMEOUT
+
+
+@pytest.mark.parametrize("flags", [0, lsgb300.NO_GRAPH])
+def test_slab_copy_wait_runs_out(flags):
+    # a negative wait limit makes every slab wait of the two-copies sweep give
+    # up at its first check: each CTA waits once more for its copies in
+    # flight, leaves, and the step reports LS_DEVICE_TIMEOUT; the handle then
+    # steps from phi0 with the normal limit and matches a fresh handle
+    w = synth.workload("c3", n=16)
+    ls = lsgb300.from_workload(w, flags=flags, barrier_wait_limit=-1)
+    with pytest.raises(lsgb300.LevelSetError) as e:
+        ls.step(1)
+    assert e.value.code == lsgb300.LS_DEVICE_TIMEOUT
+    p = ls.get_params()
+    p.barrier_wait_limit = 0
+    ls.set_params(p)
+    ls.setup()
+    ls.set_phi(w["phi0"])
+    h1, d1 = ls.solve(2)
+    h0, d0 = lsgb300.from_workload(w, flags=flags).solve(2)
+    assert d0 == d1 == 2
+    assert np.array_equal(h0.view(np.uint32), h1.view(np.uint32))
