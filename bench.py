@@ -33,6 +33,26 @@ import numpy as np  # noqa: E402
 
 METRIC = "narrowband vertex-updates/s (curvature flow, 128^3 jittered cube, 3 spheres)"
 UNIT = "vertex-updates/s"
+# max |phi - phi_FP64| / h of the fast build over 3 steps of this workload,
+# measured by the GPU test named in ACCURACY
+C3_FAST_MAX_ERR_H = 9.39e-5
+
+
+# the two kernel builds and what the GPU tests establish about their accuracy
+BUILDS = {
+    "fast": "fast: FMA contraction, approximate division and square root, planar-wave tet solver",
+    "bit-exact": "bit-exact: no FMA contraction, the reference's tet solver in its operand order",
+}
+ACCURACY = {
+    # printed per step by the test (3 curvature steps of this workload,
+    # against the CPU oracle run entirely in FP64)
+    "fast": {"max_err_vs_fp64_h": C3_FAST_MAX_ERR_H,
+             "source": "tests/test_gpu_configs.py::test_c3_curvature_128_cells_full_size (3 steps at 128^3, "
+                       "max |phi - phi_FP64| over the band per step, asserted <= 1e-3 h)"},
+    "bit-exact": {"equals_oracle_bitwise": True,
+                  "source": "tests/test_gpu_configs.py::test_c3_curvature_128_cells_full_size (phi, narrowband "
+                            "sets and work counters equal to the CPU oracle bit for bit over 2 steps at 128^3)"},
+}
 
 
 def job_totals(ms, updates, dist=None):
@@ -128,45 +148,99 @@ def profile_value(key):
     return None
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the FIM kernel from the committed ncu summary,
-    or None."""
-    return profile_value("traffic_bytes_per_launch")
+def profile_traffic(algorithmic_bytes_per_launch):
+    """DRAM bytes per launch of the FIM kernel: the DRAM / algorithmic byte
+    ratio of the committed ncu capture (the same launches' DRAM bytes and
+    algorithmic bytes, launch_profile.py) times this run's algorithmic bytes
+    per launch (the kernel reads a fixed slab per patch visit, so traffic
+    grows with the visits), or None."""
+    ratio = profile_value("traffic_ratio")
+    if ratio is None:
+        return None
+    return ratio * algorithmic_bytes_per_launch
+
+
+class OracleRun:
+    """CPU oracle (the FP32 port of the reference's algorithm) on the same
+    workload: warm-up steps once, then timed samples from the warm state
+    with any thread count (each sample's first step seeds over all
+    patches, as a fresh reference GenerateData call does)."""
+
+    def __init__(self, w, warm, threads, precision=32):
+        import lsoracle
+
+        self.w = w
+        self.ol = lsoracle.OracleLayout(w["dim"], w["xyz"], w["elems"], w["npart"], w["nparts"])
+        self.kind = lsoracle.UPDATE[w["update"]]
+        self.precision = precision
+        self.phi = w["phi0"]
+        if warm > 0:
+            hist, _, _, _ = self.ol.solve(self._params(threads), w["phi0"], w["vel"], warm, nb_sets=False)
+            self.phi = hist[-1]
+
+    def _params(self, threads):
+        w = self.w
+        return self.ol.params(update_kind=self.kind, dt=w["dt"], bandwidth=w["bandwidth"], curv_coeff=1.0,
+                              nthreads=threads, precision=self.precision)
+
+    def rate(self, nsteps, threads):
+        """(vertex-updates/s, seconds, stats) of nsteps timed steps."""
+        t0 = time.perf_counter()
+        _, _, _, st = self.ol.solve(self._params(threads), self.phi, self.w["vel"], nsteps, nb_sets=False)
+        sec = time.perf_counter() - t0
+        return st["nb_vertex_updates"] / sec, sec, st
 
 
 def oracle_rate(w, nsteps, warm, threads, precision=32):
-    """CPU oracle (port of the reference's algorithm) on the same workload:
-    `warm` untimed steps then `nsteps` timed steps."""
-    import lsoracle
+    """`warm` untimed steps then `nsteps` timed steps of the CPU oracle."""
+    return OracleRun(w, warm, threads, precision).rate(nsteps, threads)
 
-    ol = lsoracle.OracleLayout(w["dim"], w["xyz"], w["elems"], w["npart"], w["nparts"])
-    kind = lsoracle.UPDATE[w["update"]]
-    p = ol.params(update_kind=kind, dt=w["dt"], bandwidth=w["bandwidth"], curv_coeff=1.0, nthreads=threads,
-                  precision=precision)
-    hist, _, _, s0 = ol.solve(p, w["phi0"], w["vel"], warm, nb_sets=False)
-    phi = hist[-1]
-    # the timed run continues from the warm state (its first step seeds over
-    # all patches, as a fresh reference GenerateData call does)
-    t0 = time.perf_counter()
-    _, _, _, s1 = ol.solve(p, phi, w["vel"], nsteps, nb_sets=False)
-    sec = time.perf_counter() - t0
-    return s1["nb_vertex_updates"] / sec, sec, s1
+
+# wall-clock budget of the reference arm's timed steps (the oracle port takes
+# about 1.2 s per 128^3 step on 16 Grace cores): the requested step count
+# runs whole unless it would exceed this
+REFERENCE_BUDGET_S = 180.0
+
+
+def one_core_sample(run, per_step_s_multi, threads):
+    """One step of the same oracle on one host core (the reference's own CPU
+    code is single-threaded), from the same warm state."""
+    rate1, sec1, _ = run.rate(1, 1)
+    return {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "1 timed step of the full workload from the warm state, FP32 oracle port, 1 thread "
+                      "(%.1f s; %d threads: %.2f s per step)" % (sec1, threads, per_step_s_multi)}
 
 
 def run_reference_arm(args, w, rank):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    k = min(args.steps, 5)
-    warm = min(args.warmup, 1)
-    rate, sec, st = oracle_rate(w, k, warm, threads)
-    sample = "%d timed steps after %d warm-up step(s) of the full workload, FP32 oracle port, %d threads" % (k, warm, threads)
+    warm = max(args.warmup, 0)
+    t0 = time.perf_counter()
+    run = OracleRun(w, warm, threads)
+    warm_s = time.perf_counter() - t0
+    # the requested steps, unless the measured warm-up rate says they would
+    # exceed the budget
+    per_step = warm_s / warm if warm > 0 else 0.0
+    k = args.steps
+    note = None
+    if per_step > 0 and per_step * k > REFERENCE_BUDGET_S:
+        k = max(1, int(REFERENCE_BUDGET_S / per_step))
+        note = "%d of the %d requested steps: %.1f s per step would exceed the %.0f s budget" % (
+            k, args.steps, per_step, REFERENCE_BUDGET_S)
+    rate, sec, st = run.rate(k, threads)
+    sample = "%d timed steps after %d warm-up step(s) of the full workload, FP32 oracle port, %d threads" % (
+        k, warm, threads)
+    cfg = {"workload": w["label"], "steps_requested": args.steps, "steps_run": k}
+    if note:
+        cfg["note"] = note
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
         "warmup": warm, "ms_per_step": 1000.0 * sec / k, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered cube, sphere-union SDF)",
-        "config": {"workload": w["label"], "steps_requested": args.steps},
+        "config": cfg,
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline_1core": one_core_sample(run, sec / k, threads),
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -330,6 +404,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=128, help="cells per side (128 = the benchmark workload)")
     ap.add_argument("--fp64-flagged", action="store_true", help="precision form")
+    ap.add_argument("--bit-exact", action="store_true",
+                    help="the bit-exact kernel build (no FMA contraction, the reference's tet solver), which "
+                         "equals the CPU oracle bit for bit")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 5 = two element copies per thread; 0 = library default)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -347,7 +424,7 @@ def main():
     import synth
 
     w = synth.workload("c3", seed=0, n=args.n)
-    w["label"] = "c3 curvature flow %d^3 cells x 6 tets (%d verts, %d tets), w=6h, dt=0.5h^2, 3x3x3-vertex patches" % (
+    w["label"] = "c3 curvature flow %d^3 cells x 6 tets (%d verts, %d tets), w=6h, dt=0.5h^2" % (
         w["n"], len(w["xyz"]), len(w["elems"]))
     if args.impl == "reference":
         return run_reference_arm(args, w, rank)
@@ -365,11 +442,11 @@ def main():
     extra = {"fim_ctas_per_sm": args.ctas} if args.ctas else {}
     tune = None
     if args.no_autotune:
-        ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged, **extra)
+        ls = lsgb300.from_workload(w, fp64_flagged=args.fp64_flagged, bit_exact=args.bit_exact, **extra)
     else:
         # structured blocks of a tuned side (the autotuner times 2 steps per
         # candidate patch size and CTAs-per-SM setting, from phi0)
-        flags = lsgb300.FP64_FLAGGED if args.fp64_flagged else 0
+        flags = (lsgb300.FP64_FLAGGED if args.fp64_flagged else 0) | (lsgb300.BITEXACT if args.bit_exact else 0)
         p = lsgb300.default_params(time_step=w["dt"], bandwidth=w["bandwidth"], update_kind=lsgb300.UPDATE_CURVATURE,
                                    curv_coeff=1.0, partition_type=1, side_lengths=w["n"] + 1, block_size=3,
                                    flags=flags, **extra)
@@ -381,8 +458,6 @@ def main():
         tp = ls.get_params()
         tune = {"patch_side_vertices": tp.block_size, "fim_ctas_per_sm": tp.fim_ctas_per_sm,
                 "trials": [[t["patch_size"], t["fim_ctas_per_sm"], round(t["ms_per_step"], 3)] for t in trials]}
-        w["label"] = w["label"].replace("3x3x3-vertex patches", "%dx%dx%d-vertex patches (autotuned)" % (
-            (tp.block_size,) * 3))
     nv = len(w["xyz"])
     # L2 flush buffer (larger than the 129 MB L2), written between timed steps
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -457,7 +532,12 @@ def main():
     # setting 5 (patches of up to 384 copies), one per thread otherwise
     sweep_kernel = "k_fim_pair" if ls.get_params().fim_ctas_per_sm == 5 else "k_fim_compact"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profile_traffic(), "kernel": sweep_kernel + " (FIM patch sweep and check launches)",
+                "traffic": profile_traffic(bytes_per_launch),
+                "kernel": sweep_kernel + " (FIM patch sweep and check launches)",
+                "traffic_source": "this run's algorithmic bytes per launch x the DRAM/algorithmic ratio of an ncu "
+                                  "capture (dram__bytes_read.sum + dram__bytes_write.sum) of this kernel build's "
+                                  "first FIM launches at 96^3, profiles/k_fim_sweep_c3.md",
+                "traffic_ratio": profile_value("traffic_ratio"),
                 "peak_source": peak_kind,
                 "share_of_step": ((ps["ms_sweep"] + ps["ms_check"]) / step_ms_prof) if step_ms_prof > 0 else None,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": sweep_ms,
@@ -468,11 +548,14 @@ def main():
                 "issue_slots_active": profile_value("issue_slots_active")}
 
     cpu = None
+    cpu1 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, sec, _ = oracle_rate(w, 2, 1, threads)
+        run = OracleRun(w, 1, threads)
+        rate, sec, _ = run.rate(2, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "2 timed steps after 1 warm-up step of the full workload, FP32 oracle port (%.1f s)" % sec}
+        cpu1 = one_core_sample(run, sec / 2, threads)
 
     if rank == 0:
         line = {
@@ -488,6 +571,9 @@ def main():
                        "nb_patches_per_step": st["nb_patches"] / args.steps,
                        "flagged_fp64_solves": st["flagged_copies"],
                        "kernel_ms_per_step_profiled": kernel_ms,
+                       "patch_side_vertices": ls.get_params().block_size,
+                       "build": BUILDS["bit-exact" if args.bit_exact else "fast"],
+                       "accuracy": ACCURACY["bit-exact" if args.bit_exact else "fast"],
                        "autotune": tune},
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 4 * nv, "d2h_bytes_per_step": 4 * nv,
@@ -495,6 +581,7 @@ def main():
             "gpu_launches": gpu_launches,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "cpu_baseline_1core": cpu1,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -208,6 +208,17 @@ ls_status ls_get_phi(ls_handle* h, float* phi);
 ls_status ls_get_stats(ls_handle* h, ls_stats* s);
 /* Zeroes the counters and drops profiled kernel times not yet read. */
 ls_status ls_reset_stats(ls_handle* h);
+/* Per-launch record of the FIM patch kernel (no counterpart in the
+ * reference, whose host loop times nothing): for every sweep and check
+ * launch of the profiled steps (LS_PROFILE / ls_set_profile) since the last
+ * ls_reset_stats, oldest first, its kind (0 sweep, or the whole FIM loop of
+ * a step with LS_PERSISTENT; 1 neighbour check), its device time in ms
+ * (CUDA events on the handle's stream) and its algorithmic slab bytes (the
+ * per-visit bytes of every patch visit and check it ran; -1 past 4,096
+ * launches in one step).  Copies min(cap, available) records into the
+ * caller's arrays (any of them may be NULL) and the number available into
+ * *n.  At most 2^20 records are kept. */
+ls_status ls_get_launch_log(ls_handle* h, int cap, int* kinds, double* ms, long long* bytes, int* n);
 /* Turn per-kernel CUDA-event timing on or off for the following steps
  * (kernels are then launched one by one instead of from the graph). */
 ls_status ls_set_profile(ls_handle* h, int on);

@@ -464,6 +464,21 @@ ls_status ls_reset_stats(ls_handle* h) {
   return LS_OK;
 }
 
+ls_status ls_get_launch_log(ls_handle* h, int cap, int* kinds, double* ms, long long* bytes, int* n) {
+  if (!h || !n || cap < 0) return LS_BAD_INPUT;
+  *n = 0;
+  if (!h->solver) return LS_OK;
+  const std::vector<lsgb::LaunchRec>& log = h->solver->launch_log();
+  *n = (int)log.size();
+  const int k = std::min(cap, *n);
+  for (int i = 0; i < k; ++i) {
+    if (kinds) kinds[i] = log[i].kind;
+    if (ms) ms[i] = log[i].ms;
+    if (bytes) bytes[i] = log[i].bytes;
+  }
+  return LS_OK;
+}
+
 ls_status ls_get_narrowband(ls_handle* h, unsigned char* flags) {
   if (!h || !flags) return LS_BAD_INPUT;
   if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");

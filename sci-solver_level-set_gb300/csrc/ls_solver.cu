@@ -45,6 +45,7 @@ Solver::~Solver() {
   if (h_counts_) cudaFreeHost(h_counts_);
   if (h_stats_) cudaFreeHost(h_stats_);
   if (h_stage_) cudaFreeHost(h_stage_);
+  if (h_snap_) cudaFreeHost(h_snap_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
   for (auto& pe : prof_) {
@@ -76,13 +77,54 @@ cudaError_t Solver::prof_begin(ProfEvent& pe, int kind) {
   return cudaSuccess;
 }
 
+// A profiled FIM launch: events around it as for the other kernels, and the
+// slab-byte counter copied (on the stream, device to device) just before
+// and just after it, outside the event pair.
+cudaError_t Solver::prof_fim_begin(ProfEvent& pe, int kind) {
+  cudaError_t e = prof_begin(pe, kind);
+  if (e != cudaSuccess) return e;
+  pe.snap = -1;
+  if (!d_snap_) {
+    long long* d = nullptr;
+    e = dalloc(allocs_, &d, (size_t)2 * kSnapCap);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&h_snap_, sizeof(long long) * 2 * kSnapCap);
+    if (e != cudaSuccess) return e;
+    d_snap_ = d;
+  }
+  if (nsnap_ < kSnapCap) {
+    pe.snap = nsnap_++;
+    e = cudaMemcpyAsync(d_snap_ + 2 * pe.snap, s_.stats + 7, sizeof(long long), cudaMemcpyDeviceToDevice, stream_);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaEventRecord(pe.a, stream_);
+}
+
+cudaError_t Solver::prof_fim_end(ProfEvent& pe) {
+  cudaError_t e = cudaEventRecord(pe.b, stream_);
+  if (e == cudaSuccess && pe.snap >= 0)
+    e = cudaMemcpyAsync(d_snap_ + 2 * pe.snap + 1, s_.stats + 7, sizeof(long long), cudaMemcpyDeviceToDevice,
+                        stream_);
+  prof_.push_back(pe);
+  return e;
+}
+
 // Adds the pending launch times to the stats (keep_times) or drops them, and
-// returns their events to the pool.
+// returns their events to the pool; FIM launches also go to the launch log
+// with their slab bytes.
 void Solver::fold_prof(bool keep_times) {
+  bool snaps = false;
+  if (keep_times && nsnap_ > 0)
+    snaps = cudaMemcpyAsync(h_snap_, d_snap_, sizeof(long long) * 2 * nsnap_, cudaMemcpyDeviceToHost, stream_) ==
+                cudaSuccess &&
+            cudaStreamSynchronize(stream_) == cudaSuccess;
+  nsnap_ = 0;
   for (auto& pe : prof_) {
     float ms = 0;
     if (keep_times && cudaEventSynchronize(pe.b) == cudaSuccess &&
         cudaEventElapsedTime(&ms, pe.a, pe.b) == cudaSuccess) {
+      if (pe.kind <= 1 && launch_log_.size() < kLaunchLogCap)
+        launch_log_.push_back(
+            {pe.kind, (double)ms, (snaps && pe.snap >= 0) ? h_snap_[2 * pe.snap + 1] - h_snap_[2 * pe.snap] : -1});
       switch (pe.kind) {
         case 0: st_.ms_sweep += ms; st_.n_sweep++; break;
         case 1: st_.ms_check += ms; st_.n_check++; break;
@@ -454,13 +496,11 @@ std::string Solver::fim_loop(const StepParams& sp) {
   auto prof = [&](int kind, auto&& fn) -> cudaError_t {
     if (!cfg_.profile) return fn();
     ProfEvent pe;
-    cudaError_t e = prof_begin(pe, kind);
+    cudaError_t e = prof_fim_begin(pe, kind);
     if (e != cudaSuccess) return e;
-    cudaEventRecord(pe.a, stream_);
     e = fn();
-    cudaEventRecord(pe.b, stream_);
-    prof_.push_back(pe);
-    return e;
+    cudaError_t e2 = prof_fim_end(pe);
+    return e != cudaSuccess ? e : e2;
   };
   // a wait of the FIM kernels that runs out sets ctl[3] (read at every sync)
   LS_TRY(cudaMemsetAsync(s_.ctl + 3, 0, sizeof(int), stream_), "memset");
@@ -530,15 +570,9 @@ std::string Solver::one_step(bool* empty_nb) {
     // the persistent step launch by launch (profiled: the FIM loop kernel's
     // time is recorded as the sweep time)
     ProfEvent pe{};
-    if (cfg_.profile) {
-      LS_TRY(prof_begin(pe, 0), "event");
-      LS_TRY(cudaEventRecord(pe.a, stream_), "event");
-    }
+    if (cfg_.profile) LS_TRY(prof_fim_begin(pe, 0), "event");
     LS_TRY(step_persistent_launches(use_all), "persistent step");
-    if (cfg_.profile) {
-      LS_TRY(cudaEventRecord(pe.b, stream_), "event");
-      prof_.push_back(pe);
-    }
+    if (cfg_.profile) LS_TRY(prof_fim_end(pe), "event");
     LS_TRY(cudaMemcpyAsync(h_counts_, s_.counts, sizeof(int) * 8, cudaMemcpyDeviceToHost, stream_), "d2h");
     LS_TRY(cudaMemcpyAsync(h_counts_ + 8, s_.ctl, sizeof(int) * 4, cudaMemcpyDeviceToHost, stream_), "d2h");
     LS_TRY(cudaStreamSynchronize(stream_), "step sync");
@@ -947,6 +981,7 @@ void Solver::reset_stats() {
   cudaStreamSynchronize(stream_);
   // launch times recorded before the reset are dropped with the counters
   fold_prof(false);
+  launch_log_.clear();
   st_ = SolverStats();
   stats_stale_ = false;
 }

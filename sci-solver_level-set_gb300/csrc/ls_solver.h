@@ -95,6 +95,14 @@ struct SolverStats {
   long long early_visits = 0;
 };
 
+// One profiled FIM launch: 0 sweep (or the persistent FIM loop), 1 check;
+// device time; algorithmic slab bytes (-1 when not recorded).
+struct LaunchRec {
+  int kind;
+  double ms;
+  long long bytes;
+};
+
 class Solver {
  public:
   Solver() = default;
@@ -114,6 +122,13 @@ class Solver {
   std::string dt_values(float* dt_new_order);
   void stats(SolverStats& s);  // reads the device counters if a step ran since the last read
   void reset_stats();
+  // FIM launches of the profiled steps since the last reset_stats (oldest
+  // first, at most kLaunchLogCap kept)
+  const std::vector<LaunchRec>& launch_log() {
+    if (stats_stale_) pull_stats();
+    return launch_log_;
+  }
+  static constexpr size_t kLaunchLogCap = 1u << 20;
   int status_code() const { return status_; }
   void set_profile(bool on) { cfg_.profile = on ? 1 : 0; }
   // Learned warm start: each step's FIM starts from |network prediction| +
@@ -143,10 +158,21 @@ class Solver {
   struct ProfEvent {
     cudaEvent_t a, b;
     int kind;
+    int snap = -1;  // FIM launches: slot of the slab-byte counter snapshots around the launch
   };
   std::vector<ProfEvent> prof_;
+  std::vector<LaunchRec> launch_log_;
   std::vector<cudaEvent_t> ev_pool_;
   cudaError_t prof_begin(ProfEvent& pe, int kind);
+  // profiled FIM launches: the device's slab-byte counter (stats[7]) copied
+  // before and after each launch into d_snap_ (slots of 2, at most kSnapCap
+  // launches between two folds), read back when the times are folded
+  static constexpr int kSnapCap = 4096;
+  long long* d_snap_ = nullptr;
+  long long* h_snap_ = nullptr;
+  int nsnap_ = 0;
+  cudaError_t prof_fim_begin(ProfEvent& pe, int kind);
+  cudaError_t prof_fim_end(ProfEvent& pe);
   void fold_prof(bool keep_times);
 
   const Layout* lay_ = nullptr;

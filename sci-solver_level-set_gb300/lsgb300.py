@@ -64,7 +64,7 @@ class Stats(ctypes.Structure):
 EXPORTS = [
     "ls_default_params", "ls_create", "ls_destroy", "ls_set_params", "ls_get_params", "ls_set_mesh",
     "ls_set_partition", "ls_set_phi", "ls_set_velocity", "ls_prepare", "ls_setup", "ls_solve", "ls_step",
-    "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_narrowband",
+    "ls_step_host", "ls_get_phi", "ls_get_stats", "ls_reset_stats", "ls_get_launch_log", "ls_get_narrowband",
     "ls_get_layout_info", "ls_get_layout", "ls_last_error", "ls_version", "ls_partition_structured",
     "ls_partition_rcb", "ls_set_profile", "ls_debug_active", "ls_narrowband_noalloc", "ls_load_mesh",
     "ls_get_mesh_info", "ls_get_mesh", "ls_write_vtk", "ls_eikonal", "ls_batch_create", "ls_batch_destroy",
@@ -114,6 +114,7 @@ def lib():
     L.ls_get_phi.argtypes = [P, V]
     L.ls_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
     L.ls_reset_stats.argtypes = [P]
+    L.ls_get_launch_log.argtypes = [P, I, V, V, V, ctypes.POINTER(I)]
     L.ls_set_profile.argtypes = [P, I]
     L.ls_debug_active.argtypes = [P, V, I, ctypes.POINTER(I), V]
     L.ls_load_mesh.argtypes = [P, ctypes.c_char_p]
@@ -362,6 +363,21 @@ class LevelSet:
 
     def reset_stats(self):
         self._check(lib().ls_reset_stats(self._h), "reset_stats")
+
+    def launch_log(self):
+        """FIM kernel launches of the profiled steps since the last
+        reset_stats: (kinds [0 sweep, 1 check], device ms, algorithmic slab
+        bytes) as numpy arrays."""
+        n = ctypes.c_int(0)
+        self._check(lib().ls_get_launch_log(self._h, 0, None, None, None, ctypes.byref(n)), "get_launch_log")
+        k = n.value
+        kinds = np.zeros(k, np.int32)
+        ms = np.zeros(k, np.float64)
+        nbytes = np.zeros(k, np.int64)
+        if k:
+            self._check(lib().ls_get_launch_log(self._h, k, _ptr(kinds), _ptr(ms), _ptr(nbytes), ctypes.byref(n)),
+                        "get_launch_log")
+        return kinds, ms, nbytes
 
     def narrowband(self, nparts):
         out = np.zeros(nparts, np.uint8)

@@ -319,3 +319,24 @@ def test_slab_copy_wait_runs_out(flags):
     h0, d0 = lsgb300.from_workload(w, flags=flags).solve(2)
     assert d0 == d1 == 2
     assert np.array_equal(h0.view(np.uint32), h1.view(np.uint32))
+
+
+@pytest.mark.parametrize("flags", [0, lsgb300.PERSISTENT])
+def test_launch_log_sums_to_profiled_totals(flags):
+    # per-launch records of the profiled FIM launches: as many as the
+    # profiled sweep and check launches, their times and algorithmic bytes
+    # summing to the stats' totals
+    w = synth.workload("c3", n=20)
+    ls = lsgb300.from_workload(w, flags=flags)
+    ls.step(1)
+    ls.set_profile(True)
+    ls.reset_stats()
+    ls.step(2)
+    kinds, ms, nbytes = ls.launch_log()
+    st = ls.stats()
+    assert len(kinds) == st["n_sweep"] + st["n_check"] > 0
+    assert (kinds == 0).sum() == st["n_sweep"] and (kinds == 1).sum() == st["n_check"]
+    assert (nbytes >= 0).all() and nbytes.sum() == st["sweep_slab_bytes"]
+    assert abs(ms.sum() - (st["ms_sweep"] + st["ms_check"])) < 1e-3 * max(1.0, ms.sum())
+    ls.reset_stats()
+    assert len(ls.launch_log()[0]) == 0
