@@ -251,7 +251,9 @@ def run_batched(args, rank, world, local):
     """64 independent jittered cubes (16..64 cells per side, log-uniform),
     advection by random rigid rotations, stepped as one batch (one patch set,
     one launch sequence per step) and, for comparison, one handle per mesh
-    stepped in turn on the same GPU."""
+    stepped in turn on the same GPU.  With --learned the batch runs with the
+    learned warm start (network trained first, train_network), next to the
+    plain batch."""
     import lsgb300
     import synth
     import torch
@@ -263,25 +265,52 @@ def run_batched(args, rank, world, local):
     nv = sum(len(w["xyz"]) for w in ws)
     ne = sum(len(w["elems"]) for w in ws)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    b = lsgb300.LevelSetBatch()
-    for w in ws:
-        b.add(lsgb300.from_workload(w, setup=False))
-    b.setup()
-    for _ in range(args.warmup):
-        b.solve(1)
-    b.reset_stats()
-    clocks = ClockSampler(local)
-    clocks.start()
-    ms = 0.0
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        before = b.stats()["ms_total"]
-        b.solve(1)
-        ms += b.stats()["ms_total"] - before
-    clocks.stop()
-    st = b.stats()
+    net, training = (train_network(args.n) if args.learned else (None, None))
+
+    def run_batch(learned):
+        b = lsgb300.LevelSetBatch()
+        for w in ws:
+            b.add(lsgb300.from_workload(w, setup=False))
+        b.setup()
+        if learned:
+            b.set_learned(net, margin=0.3, reset_mode=0)
+        for _ in range(args.warmup):
+            b.solve(1)
+        b.reset_stats()
+        clocks = ClockSampler(local)
+        clocks.start()
+        ms = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            before = b.stats()["ms_total"]
+            b.solve(1)
+            ms += b.stats()["ms_total"] - before
+        clocks.stop()
+        st = b.stats()
+        phis = [b.phi(i) for i in range(len(ws))]
+        b.close()
+        return ms, st, clocks.summary(), phis
+
+    learned_part = None
+    if args.learned:
+        ms_l, st_l, clk_l, ph_l = run_batch(True)
+    ms, st, clk, ph = run_batch(False)
     value = st["nb_vertex_updates"] / (ms / 1000.0)
+    if args.learned:
+        value_l = st_l["nb_vertex_updates"] / (ms_l / 1000.0)
+        diff = 0.0
+        for w, a, c in zip(ws, ph_l, ph):
+            band = np.abs(c) <= w["bandwidth"]
+            if band.any():
+                diff = max(diff, float(np.max(np.abs(a[band] - c[band])) / w["h"]))
+        learned_part = {"value": value_l, "unit": UNIT, "ms_per_step": ms_l / args.steps, "clocks": clk_l,
+                        "training": training, "warm_vertices": st_l["warm_vertices"],
+                        "moved_beyond_1e-3h": st_l["moved_vertices"], "unsupported_resets": st_l["unsupported_resets"],
+                        "support_rounds": st_l["support_rounds"], "fallbacks_to_plain": st_l["learned_fallbacks"],
+                        "patch_visits_per_step": st_l["patch_visits"] / args.steps,
+                        "learned_batched_over_plain_batched": value_l / value,
+                        "max_abs_diff_vs_plain_h": diff}
     # the same meshes one handle at a time (the reference's one-mesh-per-solver use)
     seq_ms, seq_updates = 0.0, 0
     for w in ws:
@@ -310,7 +339,8 @@ def run_batched(args, rank, world, local):
         "sequential": {"value": seq_value, "unit": UNIT, "ms_per_step": seq_ms / args.steps,
                        "how": "one handle per mesh, meshes stepped in turn, same steps"},
         "batched_over_sequential": value / seq_value,
-        "clocks": clocks.summary(),
+        "learned": learned_part,
+        "clocks": clk,
         "e2e": None,
         "gpu_launches": int(st["kernel_launches"]),
     }
@@ -318,12 +348,66 @@ def run_batched(args, rank, world, local):
     return 0
 
 
+# training pairs (features of a vertex before the redistance, its signed
+# distance / h after it) from this project's own FIM: seeded runs of the
+# 3D-advection and curvature-flow families, other seeds than the benchmark's
+PAIR_SOURCES = (  # (family, cells per side, seed, pairs to collect)
+    ("c3", 128, 1, 9_000_000), ("c3", 128, 2, 9_000_000), ("c2", 32, 3, 1_500_000), ("c2", 32, 4, 1_500_000))
+PAIR_CAPACITY = 24 * 1024 * 1024
+TRAIN_EPOCHS, TRAIN_BATCH, TRAIN_LR = 20, 65536, 1e-3
+
+
+def train_network(n_eval):
+    """Collects about 21 M training pairs (PAIR_SOURCES), trains the network
+    on the GPU (Adam, batch 65,536), and measures its error on pairs of the
+    benchmark workload (seed 0, n_eval^3 cells) that it was not trained on."""
+    import lsgb300
+    import synth
+
+    m = lsgb300.MLP(11)
+    m.reserve_pairs(PAIR_CAPACITY)
+    t0 = time.perf_counter()
+    sources = []
+    for name, n, seed, quota in PAIR_SOURCES:
+        ls = lsgb300.from_workload(synth.workload(name, n=n, seed=seed))
+        start = m.num_pairs()
+        steps = 0
+        while m.num_pairs() - start < quota and steps < 100:
+            ls.learn_collect(m, 4)
+            steps += 4
+        sources.append({"workload": "%s %d^3 seed %d" % (name, n, seed), "steps": steps,
+                        "pairs": m.num_pairs() - start})
+        ls.close()
+    collect_s = time.perf_counter() - t0
+    npairs = m.num_pairs()
+    t0 = time.perf_counter()
+    loss = m.train_pairs(epochs=TRAIN_EPOCHS, batch=TRAIN_BATCH, lr=TRAIN_LR, seed=1)
+    train_s = time.perf_counter() - t0
+    # held-out error: pairs of the benchmark workload, appended after training
+    first = m.num_pairs()
+    ls = lsgb300.from_workload(synth.workload("c3", n=n_eval, seed=0))
+    ls.learn_collect(m, 4)
+    ls.close()
+    err = m.eval_pairs(first, m.num_pairs() - first)
+    q = lambda x: float(np.quantile(err, x)) if err.size else None  # noqa: E731
+    info = {"pairs": npairs, "sources": sources, "collect_s": collect_s, "train_s": train_s,
+            "epochs": TRAIN_EPOCHS, "batch": TRAIN_BATCH, "lr": TRAIN_LR, "last_epoch_loss": loss,
+            "batches": TRAIN_EPOCHS * ((npairs + TRAIN_BATCH - 1) // TRAIN_BATCH),
+            "ms_per_batch": 1000.0 * train_s / max(1, TRAIN_EPOCHS * ((npairs + TRAIN_BATCH - 1) // TRAIN_BATCH)),
+            "held_out": {"workload": "c3 %d^3 seed 0, 4 steps" % n_eval, "pairs": int(err.size),
+                         "abs_err_h": {"p50": q(0.5), "p90": q(0.9), "p99": q(0.99),
+                                       "max": float(err.max()) if err.size else None},
+                         "frac_within_h": {"1e-3": float((err <= 1e-3).mean()) if err.size else None,
+                                           "1e-2": float((err <= 1e-2).mean()) if err.size else None,
+                                           "1e-1": float((err <= 1e-1).mean()) if err.size else None}}}
+    return m, info
+
+
 def run_learned(args, rank, world, local):
-    """The curvature-flow workload with the learned warm start: training
-    pairs from this project's FIM on seeded 32^3 and 48^3 curvature-flow and
-    torus-advection runs, the network trained on the GPU, then timed steps at
-    --n cells per side with the warm start (margin 0.3 h, whole-patch resets)
-    next to the same steps of the plain path."""
+    """The curvature-flow workload with the learned warm start: the network
+    trained on the GPU (train_network), then timed steps at --n cells per
+    side with the warm start (margin 0.3 h, whole-patch resets) next to the
+    same steps of the plain path."""
     import lsgb300
     import synth
     import torch
@@ -331,17 +415,7 @@ def run_learned(args, rank, world, local):
     if world > 1 and rank != 0:
         return 0
     torch.cuda.set_device(local)
-    m = lsgb300.MLP(11)
-    m.reserve_pairs(1 << 23)
-    t0 = time.perf_counter()
-    for name, n, seed in (("c3", 32, 1), ("c3", 48, 2), ("c2", 32, 3), ("c3", 48, 4)):
-        ls = lsgb300.from_workload(synth.workload(name, n=n, seed=seed))
-        ls.learn_collect(m, 16)
-        ls.close()
-    collect_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    loss = m.train_pairs(epochs=20, batch=65536, lr=1e-3, seed=1)
-    train_s = time.perf_counter() - t0
+    m, training = train_network(args.n)
     w = synth.workload("c3", seed=0, n=args.n)
     nv = len(w["xyz"])
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -380,8 +454,7 @@ def run_learned(args, rank, world, local):
         "dtype": "f32 (network bf16, fp32 accumulate)", "data": "synthetic (seeded jittered cube, sphere-union SDF)",
         "config": {"workload": "c4 learned warm start on c3 %d^3 (%d verts)" % (w["n"], nv),
                    "l2": "flushed between timed steps (256 MB write)",
-                   "training": {"pairs": m.num_pairs(), "collect_s": collect_s, "train_s": train_s,
-                                "last_epoch_loss": loss, "epochs": 20, "batch": 65536},
+                   "training": training,
                    "warm_vertices": st_l["warm_vertices"], "moved_beyond_1e-3h": st_l["moved_vertices"],
                    "unsupported_resets": st_l["unsupported_resets"], "support_rounds": st_l["support_rounds"],
                    "fallbacks_to_plain": st_l["learned_fallbacks"],
@@ -411,6 +484,8 @@ def main():
     ap.add_argument("--ctas", type=int, default=0, help="FIM CTAs per SM (2, 3, 4; 5 = two element copies per thread; 0 = library default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep 3x3x3-vertex patches and the default FIM CTAs per SM instead of the autotuner's pick")
+    ap.add_argument("--learned", action="store_true",
+                    help="c5: also run the batch with the learned warm start (the network is trained first)")
     ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5"],
                     help="c3: the 128^3 curvature-flow benchmark; c4: the same with the learned warm start; "
                          "c5: 64 independent meshes as one batch")

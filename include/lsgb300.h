@@ -393,6 +393,11 @@ ls_status ls_mlp_clear_pairs(ls_mlp* m);
 ls_status ls_mlp_num_pairs(ls_mlp* m, long long* n);
 ls_status ls_mlp_train_pairs(ls_mlp* m, int epochs, int batch, float lr, unsigned long long seed, float* loss);
 ls_status ls_learn_collect(ls_handle* h, ls_mlp* m, int nsteps, int* steps_done);
+/* The network's error on pairs of its buffer (no counterpart in the
+ * reference): |prediction - target| in units of h for the pairs [first,
+ * first + count), e.g. pairs collected after training from a run the
+ * network was not trained on. */
+ls_status ls_mlp_eval_pairs(ls_mlp* m, long long first, long long count, float* abs_err);
 /* Learned warm start for the steps of h (m = NULL turns it off): the FIM of
  * each step starts the previous narrowband's vertices at |prediction| +
  * margin (units of h, the FIM length unit) instead of LARGENUM, with all
@@ -402,9 +407,13 @@ ls_status ls_learn_collect(ls_handle* h, ls_mlp* m, int nsteps, int* steps_done)
  * its patch (reset_mode 0) or alone (reset_mode 1) -- and the FIM runs
  * again, until no such vertex is left (at most 16 rounds, then the step's
  * redistance is redone as plain FIM).  The network is not owned by h and
- * must outlive its use.  One mesh per handle (not batches); steps run
+ * must outlive its use.  Batches: ls_batch_set_learned.  Steps run
  * launch by launch. */
 ls_status ls_set_learned(ls_handle* h, ls_mlp* m, double margin, double support_tol, int reset_mode);
+/* The learned warm start for the steps of a batch (no counterpart in the
+ * reference): as ls_set_learned, with every mesh's features, predictions,
+ * margin and tolerances in units of that mesh's own h. */
+ls_status ls_batch_set_learned(ls_batch* b, ls_mlp* m, double margin, double support_tol, int reset_mode);
 
 #ifdef __cplusplus
 }

@@ -849,6 +849,11 @@ ls_status ls_mlp_train_pairs(ls_mlp* m, int epochs, int batch, float lr, unsigne
   return mfail(m, m->net.train_pairs(epochs, batch, lr, seed, loss));
 }
 
+ls_status ls_mlp_eval_pairs(ls_mlp* m, long long first, long long count, float* abs_err) {
+  if (!m || first < 0 || count < 0 || (count > 0 && !abs_err)) return LS_BAD_INPUT;
+  return mfail(m, m->net.eval_pairs(first, count, abs_err));
+}
+
 ls_status ls_learn_collect(ls_handle* h, ls_mlp* m, int nsteps, int* steps_done) {
   if (!h || !m || nsteps < 0) return LS_BAD_INPUT;
   if (!h->solver) return fail(h, LS_NOT_READY, "call ls_setup first");
@@ -857,6 +862,13 @@ ls_status ls_learn_collect(ls_handle* h, ls_mlp* m, int nsteps, int* steps_done)
   r = h->solver->run(nsteps, nullptr, steps_done);
   h->solver->set_collect(nullptr);
   return solver_status(h, r);
+}
+
+ls_status ls_batch_set_learned(ls_batch* b, ls_mlp* m, double margin, double support_tol, int reset_mode) {
+  if (!b || margin < 0 || support_tol < 0 || reset_mode < 0 || reset_mode > 1) return LS_BAD_INPUT;
+  if (!b->solver) return bfail(b, LS_NOT_READY, "call ls_batch_setup first");
+  return bsolver_status(b, b->solver->set_learned(m ? &m->net : nullptr, (float)margin, (float)support_tol,
+                                                  reset_mode == 0));
 }
 
 ls_status ls_set_learned(ls_handle* h, ls_mlp* m, double margin, double support_tol, int reset_mode) {

@@ -102,6 +102,7 @@ struct DevLearn {
   float* pred;    // network output per warm-set vertex (signed distance / h)
   float* warm;    // per vertex: warm-start value in the FIM frame
   float* target;  // collection: signed distance / h after the redistance, per warm-set vertex
+  const float* vinv_h;  // batches: per vertex, 1 / its mesh's FIM length unit (null for one mesh)
 };
 
 struct StepParams {

@@ -1831,8 +1831,9 @@ __global__ void k_moved(DevState s, DevLearn lr, float tol) {
 __global__ void k_targets(DevState s, DevLearn lr, float inv_h, float LN) {
   const int n = lr.cnt[0];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float ph = s.phi[lr.vlist[i]];
-    lr.target[i] = fabsf(ph) >= LN ? __int_as_float(0x7fc00000) : ph * inv_h;
+    const int v = lr.vlist[i];
+    const float ph = s.phi[v];
+    lr.target[i] = fabsf(ph) >= LN ? __int_as_float(0x7fc00000) : ph * (lr.vinv_h ? lr.vinv_h[v] : inv_h);
   }
 }
 

@@ -167,100 +167,150 @@ __device__ __forceinline__ uint4 pack8(const float* v) {
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-// Issue the 8 K-steps of one 128 x 128 x 128 product (thread 0 only).
-__device__ __forceinline__ void mma_tile(uint32_t tmem_d, const uint8_t* a, const uint8_t* b) {
-  const uint32_t sa = smem_u32(a), sb = smem_u32(b);
-#pragma unroll
-  for (int ks = 0; ks < F / 16; ++ks) mma(tmem_d, make_desc(sa + ks * 2 * LBO), make_desc(sb + ks * 2 * LBO), ks > 0);
-}
-
-struct Smem {
-  uint64_t bar;
-  uint32_t tmem;
-  int fail;
-};
 
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Forward.  X [n][128] BF16; W [3][128][128] BF16 ([out][in]); b [3][128],
+// Weight copies for the tensor cores: BF16 tiles in the operand layout above
+// (tile_off), so that one bulk asynchronous copy of 32 KB stages a layer's
+// weights.  Wt[l]: rows = output feature, K = input feature (B operand of
+// the forward); WTt[l]: rows = input feature, K = output feature (B operand
+// of the backward's dH = d W).
+__device__ __forceinline__ void store_weight(__nv_bfloat16* Wt, __nv_bfloat16* WTt, int i, float p) {
+  const int l = i / (F * F), o = (i / F) % F, in = i % F;
+  const __nv_bfloat16 v = __float2bfloat16_rn(p);
+  Wt[(size_t)l * F * F + tile_off(o, in) / 2] = v;
+  WTt[(size_t)l * F * F + tile_off(in, o) / 2] = v;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// one tile (32 KB, 16-byte aligned at both ends) from global into shared
+// memory, completing on bar
+__device__ __forceinline__ void bulk_tile(uint8_t* dst, const __nv_bfloat16* src, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(__cvta_generic_to_global(src)), "r"((uint32_t)TILE_BYTES), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// MMAs of one 128 x 128 x 128 product that add to the accumulator when acc
+// is set (thread 0 only)
+__device__ __forceinline__ void mma_tile_acc(uint32_t tmem_d, const uint8_t* a, const uint8_t* b, bool acc) {
+  const uint32_t sa = smem_u32(a), sb = smem_u32(b);
+#pragma unroll
+  for (int ks = 0; ks < F / 16; ++ks)
+    mma(tmem_d, make_desc(sa + ks * 2 * LBO), make_desc(sb + ks * 2 * LBO), (acc || ks > 0) ? 1 : 0);
+}
+
+struct SmemW {
+  uint64_t bar;    // MMA completion
+  uint64_t bar_w;  // weight tiles staged
+  uint32_t tmem;
+  int fail;
+};
+
+// ---------------------------------------------------------------------------
+// Forward.  X [n][128] BF16 rows; Wt the three weight tiles; b [3][128],
 // w4 [128], b4 [1] fp32; y [n]; A (optional) [3][n][128] BF16 activations
 // a_1..a_3 for the backward pass.  n_dev (optional) overrides n from device
-// memory (graph replays with a device-side sample count).
+// memory (graph replays with a device-side sample count).  Each CTA stages
+// the weights once (three bulk copies) and then runs the sample tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... through the three layers.
 __global__ void __launch_bounds__(128, 1)
-    k_mlp_fwd(const __nv_bfloat16* __restrict__ X, int n, const int* n_dev, const __nv_bfloat16* __restrict__ W,
+    k_mlp_fwd(const __nv_bfloat16* __restrict__ X, int n, const int* n_dev, const __nv_bfloat16* __restrict__ Wt,
               const float* __restrict__ b, const float* __restrict__ w4, const float* __restrict__ b4,
               float* __restrict__ y, __nv_bfloat16* __restrict__ A, int* err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* act = base;                       // activation tile (A operand)
   uint8_t* wt = base + TILE_BYTES;           // 3 weight tiles (B operands)
-  Smem* sm = reinterpret_cast<Smem*>(base + 4 * TILE_BYTES);
+  SmemW* sm = reinterpret_cast<SmemW*>(base + 4 * TILE_BYTES);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (n_dev) n = *n_dev;
-  const int s0 = blockIdx.x * TILE;
-  if (s0 >= n) return;  // whole CTA exits before any tensor-core work
+  const int ntiles = (n + TILE - 1) / TILE;
+  if ((int)blockIdx.x >= ntiles) return;  // whole CTA exits before any tensor-core work
   if (tid == 0) {
     mbar_init(&sm->bar, 1);
+    mbar_init(&sm->bar_w, 1);
     sm->fail = 0;
+    mbar_expect_tx(&sm->bar_w, 3 * TILE_BYTES);
+    for (int l = 0; l < 3; ++l) bulk_tile(wt + l * TILE_BYTES, Wt + (size_t)l * F * F, &sm->bar_w);
   }
   __syncwarp();
   if (warp == 0) tmem_alloc(&sm->tmem, 128);
-  // operands: sample row tid, weight row tid of each layer
-  const int s = s0 + tid;
-  if (s < n) load_row(act, tid, X + (size_t)s * F);
-  else zero_row(act, tid);
-  for (int l = 0; l < 3; ++l) load_row(wt + l * TILE_BYTES, tid, W + ((size_t)l * F + tid) * F);
-  fence_async_smem();
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tmem = sm->tmem;
   uint32_t phase = 0;
-  float out = 0.f;
-  bool ok = true;
-  for (int l = 0; l < 3 && ok; ++l) {
-    if (tid == 0) {
-      mma_tile(tmem, act, wt + l * TILE_BYTES);
-      mma_commit(&sm->bar);
-    }
-    ok = __syncthreads_and(mbar_wait(&sm->bar, phase)) != 0;
-    phase ^= 1;
-    if (!ok) break;
-    fence_after();
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    const int r = warp * 32 + lane;  // sample row of this thread
-    for (int c = 0; c < F / 32; ++c) {
-      float v[32];
-      tmem_ld32(trow + c * 32, v);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) v[j] = bf16r(fmaxf(v[j] + __ldg(b + l * F + c * 32 + j), 0.f));
-      if (l < 2) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4*>(act + tile_off(r, c * 32 + q * 8)) = pack8(v + q * 8);
-      } else {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) out += v[j] * __ldg(w4 + c * 32 + j);
-      }
-      if (A && s0 + r < n) {
-        uint4* dst = reinterpret_cast<uint4*>(A + ((size_t)l * n + s0 + r) * F + c * 32);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) dst[q] = pack8(v + q * 8);
-      }
-    }
-    fence_before();
+  bool ok = true, weights = false, mma_pending = false;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int s0 = tile * TILE;
+    const int s = s0 + tid;  // sample row tid of the operand tile
+    if (s < n) load_row(act, tid, X + (size_t)s * F);
+    else zero_row(act, tid);
     fence_async_smem();
+    fence_before();
     __syncthreads();
     fence_after();
+    if (!weights) {
+      ok = __syncthreads_and(mbar_wait(&sm->bar_w, 0)) != 0;
+      weights = ok;
+      if (!ok) break;
+    }
+    float out = 0.f;
+    for (int l = 0; l < 3 && ok; ++l) {
+      if (tid == 0) {
+        mma_tile_acc(tmem, act, wt + l * TILE_BYTES, false);
+        mma_commit(&sm->bar);
+      }
+      mma_pending = true;
+      ok = __syncthreads_and(mbar_wait(&sm->bar, phase)) != 0;
+      if (!ok) break;
+      mma_pending = false;
+      phase ^= 1;
+      fence_after();
+      const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+      const int r = warp * 32 + lane;  // sample row of this thread
+      for (int c = 0; c < F / 32; ++c) {
+        float v[32];
+        tmem_ld32(trow + c * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = bf16r(fmaxf(v[j] + __ldg(b + l * F + c * 32 + j), 0.f));
+        if (l < 2) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4*>(act + tile_off(r, c * 32 + q * 8)) = pack8(v + q * 8);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) out += v[j] * __ldg(w4 + c * 32 + j);
+        }
+        if (A && s0 + r < n) {
+          uint4* dst = reinterpret_cast<uint4*>(A + ((size_t)l * n + s0 + r) * F + c * 32);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) dst[q] = pack8(v + q * 8);
+        }
+      }
+      fence_before();
+      fence_async_smem();
+      __syncthreads();
+      fence_after();
+    }
+    if (ok) {
+      const int r = warp * 32 + lane;
+      if (s0 + r < n) y[s0 + r] = out + __ldg(b4);
+    }
   }
-  if (ok) {
-    const int r = warp * 32 + lane;
-    if (s0 + r < n) y[s0 + r] = out + __ldg(b4);
-  } else {
+  if (!ok) {
     sm->fail = 1;
     if (err) atomicExch(err, 1);
-    // drain: wait (bounded) for the MMAs of this phase before freeing TMEM
-    mbar_wait(&sm->bar, phase ^ 1);
+    // drain (bounded): the weight copies and the MMAs in flight before TMEM goes
+    if (!weights) mbar_wait(&sm->bar_w, 0);
+    if (mma_pending) mbar_wait(&sm->bar, phase);
   }
   fence_before();
   __syncthreads();
@@ -269,54 +319,77 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Backward: gradients accumulated (atomics) into G = [gW (3x128x128) | gb
-// (3x128) | gw4 (128) | gb4 (1) | loss (1)], all fp32.  WT [3][in][out]
-// BF16 (transposed weights), A the forward activations, t targets.
+// Backward.  Each CTA runs the sample tiles blockIdx.x, blockIdx.x +
+// gridDim.x, ...; the three weight gradients accumulate in tensor memory
+// across its tiles (gW_l in columns [128 l, 128 l + 128), the back-propagated
+// dH of the current layer in [384, 512)); the bias, w4 and b4 gradients and
+// the loss accumulate in shared memory and registers.  At the end the CTA
+// writes its sums as row blockIdx.x of Gp [gridDim.x][NG_STRIDE], laid out as G =
+// [gW (3x128x128) | gb (3x128) | gw4 (128) | gb4 (1) | loss (1)]; k_mlp_reduce
+// adds the rows in a fixed order (no atomics in global memory, the same
+// gradient bits on every run).  WTt: the transposed weight tiles (layers 1
+// and 2 are staged once per CTA by bulk copies); A the forward activations;
+// t the targets.
+constexpr int NG_ROW = 3 * F * F + 3 * F + F + 1 + 1;
+// rows of Gp start on 16-byte boundaries (the weight gradients are stored as
+// float4)
+constexpr int NG_STRIDE = (NG_ROW + 3) & ~3;
+
 __global__ void __launch_bounds__(128, 1)
-    k_mlp_bwd(const __nv_bfloat16* __restrict__ X, int n, const __nv_bfloat16* __restrict__ WT,
+    k_mlp_bwd(const __nv_bfloat16* __restrict__ X, int n, const __nv_bfloat16* __restrict__ WTt,
               const float* __restrict__ w4, const __nv_bfloat16* __restrict__ A, const float* __restrict__ y,
-              const float* __restrict__ t, float inv_n, float* __restrict__ G, int* err) {
+              const float* __restrict__ t, float inv_n, float* __restrict__ Gp, int* err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* dT = base;                   // A operand of gW: d^T  (rows = out, K = samples)
   uint8_t* aT = base + TILE_BYTES;      // B operand of gW: a^T  (rows = in,  K = samples)
   uint8_t* dN = base + 2 * TILE_BYTES;  // A operand of dH: d    (rows = samples, K = out)
-  uint8_t* wN = base + 3 * TILE_BYTES;  // B operand of dH: W^T  (rows = in, K = out)
-  float* s_gb = reinterpret_cast<float*>(base + 4 * TILE_BYTES);  // [128] bias gradient of the layer
-  Smem* sm = reinterpret_cast<Smem*>(base + 4 * TILE_BYTES + F * sizeof(float));
+  uint8_t* wN1 = base + 3 * TILE_BYTES;  // B operand of dH for layer 1: W_1^T (rows = in, K = out)
+  uint8_t* wN2 = base + 4 * TILE_BYTES;  // the same for layer 2
+  // bias and w4 gradients, each entry owned by one thread (fixed summation
+  // order: the gradients come out the same on every run)
+  float* s_gb = reinterpret_cast<float*>(base + 5 * TILE_BYTES);  // [3][128] bias gradients
+  float* s_gw4 = s_gb + 3 * F;                                     // [128]
+  float* s_gw4w = s_gw4 + F;                                       // [4][128] the tile's per-warp w4 sums
+  float* s_red = s_gw4w + 4 * F;                                   // [2][4] per-warp gb4 and loss
+  SmemW* sm = reinterpret_cast<SmemW*>(s_red + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int s0 = blockIdx.x * TILE;
-  if (s0 >= n) return;
+  const int ntiles = (n + TILE - 1) / TILE;
+  if ((int)blockIdx.x >= ntiles) return;
   if (tid == 0) {
     mbar_init(&sm->bar, 1);
+    mbar_init(&sm->bar_w, 1);
     sm->fail = 0;
+    mbar_expect_tx(&sm->bar_w, 2 * TILE_BYTES);
+    bulk_tile(wN1, WTt + (size_t)1 * F * F, &sm->bar_w);
+    bulk_tile(wN2, WTt + (size_t)2 * F * F, &sm->bar_w);
   }
+  for (int i = tid; i < 4 * F; i += blockDim.x) s_gb[i] = 0.f;  // s_gb and s_gw4
   __syncwarp();
-  if (warp == 0) tmem_alloc(&sm->tmem, 256);
-  float* gW = G;
-  float* gb = G + 3 * F * F;
-  float* gw4 = gb + 3 * F;
-  float* gb4 = gw4 + F;
-  float* gloss = gb4 + 1;
-  const int r = tid;  // sample row of this thread in the operand phase
-  const int s = s0 + r;
-  const bool valid = s < n;
-  // output layer
-  float dy = 0.f;
-  if (valid) {
-    const float e = y[s] - t[s];
-    dy = e * inv_n;
-    atomicAdd(gloss, 0.5f * e * e * inv_n);
-  }
-  {
-    float sum = dy;
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if (lane == 0) atomicAdd(gb4, sum);
-  }
-  // d_3 = bf16(dy w4 [a_3 > 0]); gw4 = sum dy a_3
-  s_gb[tid] = 0.f;
+  if (warp == 0) tmem_alloc(&sm->tmem, 512);
+  fence_before();
   __syncthreads();
-  {
+  fence_after();
+  const uint32_t tm = sm->tmem;
+  const int r = tid;                // sample row of this thread in the operand phase
+  const int rr = warp * 32 + lane;  // accumulator row of this thread (the same index)
+  const uint32_t trow = tm + ((uint32_t)(warp * 32) << 16);
+  float gb4_acc = 0.f, loss_acc = 0.f;
+  uint32_t phase = 0;
+  bool ok = true, weights = false, mma_pending = false, first = true;
+  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int s0 = tile * TILE;
+    const int s = s0 + r;
+    const bool valid = s < n;
+    // output layer
+    float dy = 0.f;
+    if (valid) {
+      const float e = y[s] - t[s];
+      dy = e * inv_n;
+      loss_acc += 0.5f * e * e * inv_n;
+    }
+    gb4_acc += dy;
+    // d_3 = bf16(dy w4 [a_3 > 0]); its column sums are gb_3
     const __nv_bfloat16* a3 = A + ((size_t)2 * n + (valid ? s : s0)) * F;
     for (int c = 0; c < F; c += 8) {
       float av[8], dv[8];
@@ -330,116 +403,143 @@ __global__ void __launch_bounds__(128, 1)
         for (int j = 0; j < 8; ++j) av[j] = 0.f;
       }
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        dv[j] = bf16r(av[j] > 0.f ? dy * __ldg(w4 + c + j) : 0.f);
-        atomicAdd(&s_gb[c + j], dv[j]);
-      }
+      for (int j = 0; j < 8; ++j) dv[j] = bf16r(av[j] > 0.f ? dy * __ldg(w4 + c + j) : 0.f);
       *reinterpret_cast<uint4*>(dN + tile_off(r, c)) = pack8(dv);
 #pragma unroll
       for (int j = 0; j < 8; ++j) *reinterpret_cast<__nv_bfloat16*>(dT + tile_off(c + j, r)) = __float2bfloat16_rn(dv[j]);
     }
-  }
-  // gw4[j] = sum_r dy_r a3[r][j]: warp-reduce per column through shuffles
-  {
-    const __nv_bfloat16* a3 = A + ((size_t)2 * n + (valid ? s : s0)) * F;
+    // gw4[j] += sum_r dy_r a3[r][j]: warp sums through shuffles, added up
+    // per column after the next barrier
     for (int c = 0; c < F; ++c) {
       float v = valid ? dy * __bfloat162float(a3[c]) : 0.f;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) atomicAdd(gw4 + c, v);
+      if (lane == 0) s_gw4w[warp * F + c] = v;
     }
-  }
-  __syncthreads();
-  atomicAdd(gb + 2 * F + tid, s_gb[tid]);
-  uint32_t phase = 0;
-  bool ok = true;
-  for (int l = 2; l >= 0 && ok; --l) {
-    // B operand of gW_l: a_{l-1}^T (a_0 = X)
-    {
-      const __nv_bfloat16* src = l == 0 ? (X + (size_t)(valid ? s : s0) * F)
-                                        : (A + ((size_t)(l - 1) * n + (valid ? s : s0)) * F);
-      for (int c = 0; c < F; c += 8) {
-        uint4 raw = valid ? __ldg(reinterpret_cast<const uint4*>(src + c)) : make_uint4(0, 0, 0, 0);
-        const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&raw);
+    for (int l = 2; l >= 0 && ok; --l) {
+      // B operand of gW_l: a_{l-1}^T (a_0 = X)
+      {
+        const __nv_bfloat16* src = l == 0 ? (X + (size_t)(valid ? s : s0) * F)
+                                          : (A + ((size_t)(l - 1) * n + (valid ? s : s0)) * F);
+        for (int c = 0; c < F; c += 8) {
+          uint4 raw = valid ? __ldg(reinterpret_cast<const uint4*>(src + c)) : make_uint4(0, 0, 0, 0);
+          const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&raw);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) *reinterpret_cast<__nv_bfloat16*>(aT + tile_off(c + j, r)) = hb[j];
+          for (int j = 0; j < 8; ++j) *reinterpret_cast<__nv_bfloat16*>(aT + tile_off(c + j, r)) = hb[j];
+        }
       }
-    }
-    // B operand of dH_{l-1} = d_l W_l: rows of W_l^T
-    if (l > 0) load_row(wN, r, WT + ((size_t)l * F + r) * F);
-    fence_async_smem();
-    fence_before();
-    __syncthreads();
-    fence_after();
-    const uint32_t tm = sm->tmem;
-    if (tid == 0) {
-      mma_tile(tm, dT, aT);                       // gW_l  -> columns [0, 128)
-      if (l > 0) mma_tile(tm + 128, dN, wN);      // dH    -> columns [128, 256)
-      mma_commit(&sm->bar);
-    }
-    ok = __syncthreads_and(mbar_wait(&sm->bar, phase)) != 0;
-    phase ^= 1;
-    if (!ok) break;
-    fence_after();
-    const int rr = warp * 32 + lane;  // accumulator row of this thread
-    const uint32_t trow = tm + ((uint32_t)(warp * 32) << 16);
-    // gW_l row rr (output feature rr)
-    for (int c = 0; c < F / 32; ++c) {
-      float v[32];
-      tmem_ld32(trow + c * 32, v);
-      float4* dst = reinterpret_cast<float4*>(gW + ((size_t)l * F + rr) * F + c * 32);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) atomicAdd(dst + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
-    }
-    if (l > 0) {
-      // d_{l-1} for sample rr = bf16(dH * [a_{l-1} > 0])
-      s_gb[tid] = 0.f;
+      fence_async_smem();
       fence_before();
       __syncthreads();
       fence_after();
-      const int sr = s0 + rr;
-      const bool vr = sr < n;
-      const __nv_bfloat16* ap = A + ((size_t)(l - 1) * n + (vr ? sr : s0)) * F;
+      if (!weights) {
+        ok = __syncthreads_and(mbar_wait(&sm->bar_w, 0)) != 0;
+        weights = ok;
+        if (!ok) break;
+      }
+      // gb_l: thread tid sums row tid of d^T (the tile's samples in order;
+      // padding samples are zero); the tensor cores only read dT meanwhile
+      {
+        float sum = 0.f;
+        for (int k = 0; k < TILE; k += 8) {
+          const uint4 raw = *reinterpret_cast<const uint4*>(dT + tile_off(tid, k));
+          const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&raw);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) sum += __bfloat162float(hb[j]);
+        }
+        s_gb[l * F + tid] += sum;
+        if (l == 2) s_gw4[tid] += (s_gw4w[tid] + s_gw4w[F + tid]) + (s_gw4w[2 * F + tid] + s_gw4w[3 * F + tid]);
+      }
+      if (tid == 0) {
+        mma_tile_acc(tm + l * 128, dT, aT, !first);                   // gW_l (+)= d_l^T a_{l-1}
+        if (l > 0) mma_tile_acc(tm + 384, dN, l == 2 ? wN2 : wN1, false);  // dH = d_l W_l
+        mma_commit(&sm->bar);
+      }
+      mma_pending = true;
+      ok = __syncthreads_and(mbar_wait(&sm->bar, phase)) != 0;
+      if (!ok) break;
+      mma_pending = false;
+      phase ^= 1;
+      fence_after();
+      if (l > 0) {
+        // d_{l-1} for sample rr = bf16(dH * [a_{l-1} > 0]); its column sums are gb_{l-1}
+        const int sr = s0 + rr;
+        const bool vr = sr < n;
+        const __nv_bfloat16* ap = A + ((size_t)(l - 1) * n + (vr ? sr : s0)) * F;
+        for (int c = 0; c < F / 32; ++c) {
+          float v[32];
+          tmem_ld32(trow + 384 + c * 32, v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float a = vr ? __bfloat162float(ap[c * 32 + j]) : 0.f;
+            v[j] = bf16r(a > 0.f ? v[j] : 0.f);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4*>(dN + tile_off(rr, c * 32 + q * 8)) = pack8(v + q * 8);
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            *reinterpret_cast<__nv_bfloat16*>(dT + tile_off(c * 32 + j, rr)) = __float2bfloat16_rn(v[j]);
+        }
+      }
+      fence_before();
+      __syncthreads();
+      fence_after();
+    }
+    first = false;
+  }
+  if (ok) {
+    float* row = Gp + (size_t)blockIdx.x * NG_STRIDE;
+    // weight gradients: row rr of each gW_l from tensor memory
+    for (int l = 0; l < 3; ++l)
       for (int c = 0; c < F / 32; ++c) {
         float v[32];
-        tmem_ld32(trow + 128 + c * 32, v);
+        tmem_ld32(trow + l * 128 + c * 32, v);
+        float4* dst = reinterpret_cast<float4*>(row + ((size_t)l * F + rr) * F + c * 32);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const float a = vr ? __bfloat162float(ap[c * 32 + j]) : 0.f;
-          v[j] = bf16r(a > 0.f ? v[j] : 0.f);
-          atomicAdd(&s_gb[c * 32 + j], v[j]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) *reinterpret_cast<uint4*>(dN + tile_off(rr, c * 32 + q * 8)) = pack8(v + q * 8);
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-          *reinterpret_cast<__nv_bfloat16*>(dT + tile_off(c * 32 + j, rr)) = __float2bfloat16_rn(v[j]);
+        for (int q = 0; q < 8; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
       }
-      fence_before();
-      __syncthreads();
-      fence_after();
-      atomicAdd(gb + (l - 1) * F + tid, s_gb[tid]);
+    for (int o = 16; o > 0; o >>= 1) {
+      gb4_acc += __shfl_xor_sync(0xffffffffu, gb4_acc, o);
+      loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
     }
-    fence_before();
+    if (lane == 0) {
+      s_red[warp] = gb4_acc;
+      s_red[4 + warp] = loss_acc;
+    }
     __syncthreads();
-    fence_after();
-  }
-  if (!ok) {
+    for (int i = tid; i < 4 * F; i += blockDim.x) row[3 * F * F + i] = s_gb[i];  // gb and gw4
+    if (tid == 0) {
+      row[3 * F * F + 4 * F] = (s_red[0] + s_red[1]) + (s_red[2] + s_red[3]);
+      row[3 * F * F + 4 * F + 1] = (s_red[4] + s_red[5]) + (s_red[6] + s_red[7]);
+    }
+  } else {
     sm->fail = 1;
     if (err) atomicExch(err, 1);
-    mbar_wait(&sm->bar, phase ^ 1);
+    if (!weights) mbar_wait(&sm->bar_w, 0);
+    if (mma_pending) mbar_wait(&sm->bar, phase);
   }
   fence_before();
   __syncthreads();
   fence_after();
-  if (warp == 0) tmem_dealloc(sm->tmem, 256);
+  if (warp == 0) tmem_dealloc(sm->tmem, 512);
+}
+
+// G[i] = sum over the rows of Gp (fixed order); the loss of the batch is
+// also added to *loss_acc when it is given (the epoch's sum on the device).
+__global__ void k_mlp_reduce(const float* __restrict__ Gp, int rows, float* __restrict__ G, float* loss_acc) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NG_ROW; i += gridDim.x * blockDim.x) {
+    float sum = 0.f;
+    for (int r = 0; r < rows; ++r) sum += Gp[(size_t)r * NG_STRIDE + i];
+    G[i] = sum;
+    if (loss_acc && i == NG_ROW - 1) *loss_acc += sum;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Adam on the fp32 master parameters P = [W (3x128x128) | b (3x128) | w4 |
-// b4]; refreshes the BF16 copies W and W^T.
+// b4]; refreshes the BF16 weight tiles.
 __global__ void k_adam(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ M1,
                        float* __restrict__ M2, int np, float lr, float b1, float b2, float eps, float c1, float c2,
-                       __nv_bfloat16* __restrict__ Wb, __nv_bfloat16* __restrict__ WTb) {
+                       __nv_bfloat16* __restrict__ Wt, __nv_bfloat16* __restrict__ WTt) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
     const float g = G[i];
     const float m = b1 * M1[i] + (1.f - b1) * g;
@@ -448,33 +548,30 @@ __global__ void k_adam(float* __restrict__ P, const float* __restrict__ G, float
     M2[i] = v;
     const float p = P[i] - lr * (m * c1) / (sqrtf(v * c2) + eps);
     P[i] = p;
-    if (i < 3 * F * F) {
-      const int l = i / (F * F), o = (i / F) % F, in = i % F;
-      Wb[i] = __float2bfloat16_rn(p);
-      WTb[(size_t)l * F * F + (size_t)in * F + o] = __float2bfloat16_rn(p);
-    }
+    if (i < 3 * F * F) store_weight(Wt, WTt, i, p);
   }
 }
 
-__global__ void k_pack_weights(const float* __restrict__ P, __nv_bfloat16* __restrict__ Wb,
-                               __nv_bfloat16* __restrict__ WTb) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * F * F; i += gridDim.x * blockDim.x) {
-    const int l = i / (F * F), o = (i / F) % F, in = i % F;
-    Wb[i] = __float2bfloat16_rn(P[i]);
-    WTb[(size_t)l * F * F + (size_t)in * F + o] = __float2bfloat16_rn(P[i]);
-  }
+__global__ void k_pack_weights(const float* __restrict__ P, __nv_bfloat16* __restrict__ Wt,
+                               __nv_bfloat16* __restrict__ WTt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * F * F; i += gridDim.x * blockDim.x)
+    store_weight(Wt, WTt, i, P[i]);
 }
 
 // ---------------------------------------------------------------------------
 // Features of the vertices in vlist (product vertex ids): slot 0 = the vertex
 // itself (0, 0, 0, phi / h), slots 1..31 = its first 31 1-ring neighbours
-// (ascending id) as (dx, dy, dz, phi) / h, zeros beyond the ring.
+// (ascending id) as (dx, dy, dz, phi) / h, zeros beyond the ring.  h is
+// 1 / inv_h, or 1 / vinv_h[v] per vertex when given (batches of meshes of
+// different resolution).
 __global__ void k_features(int nlist, const int* __restrict__ vlist, const int* __restrict__ nlist_dev,
                            const int* __restrict__ adj_off, const int* __restrict__ adj, const float* __restrict__ xyz,
-                           int nv, const float* __restrict__ phi, float inv_h, __nv_bfloat16* __restrict__ Xo) {
+                           int nv, const float* __restrict__ phi, float inv_h, const float* __restrict__ vinv_h,
+                           __nv_bfloat16* __restrict__ Xo) {
   if (nlist_dev) nlist = *nlist_dev;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x) {
     const int v = vlist[i];
+    if (vinv_h) inv_h = vinv_h[v];
     const float x0 = xyz[v], y0 = xyz[nv + v], z0 = xyz[2 * (size_t)nv + v];
     const int a = adj_off[v], e = adj_off[v + 1];
     __nv_bfloat16* dst = Xo + (size_t)i * F;
@@ -538,8 +635,9 @@ __global__ void k_gather_pairs(const __nv_bfloat16* __restrict__ X, const float*
 namespace {
 constexpr int NP = 3 * F * F + 3 * F + F + 1;  // master parameters
 constexpr int NG = NP + 1;                      // gradients + loss
+static_assert(NG == NG_ROW, "gradient row layout");
 size_t fwd_smem() { return 4 * (size_t)TILE_BYTES + 1024 + 64; }
-size_t bwd_smem() { return 4 * (size_t)TILE_BYTES + F * sizeof(float) + 1024 + 64; }
+size_t bwd_smem() { return 5 * (size_t)TILE_BYTES + (8 * F + 8) * sizeof(float) + 1024 + 64; }
 }  // namespace
 
 #define MLP_TRY(expr, what)                                                     \
@@ -570,6 +668,15 @@ std::string Net::init(unsigned long long seed) {
   MLP_TRY(alloc((void**)&Wb_, sizeof(__nv_bfloat16) * 3 * F * F), "alloc");
   MLP_TRY(alloc((void**)&WTb_, sizeof(__nv_bfloat16) * 3 * F * F), "alloc");
   MLP_TRY(alloc((void**)&err_, sizeof(int)), "alloc");
+  MLP_TRY(alloc((void**)&loss_acc_, sizeof(float)), "alloc");
+  {
+    int dev = 0;
+    MLP_TRY(cudaGetDevice(&dev), "device");
+    MLP_TRY(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev), "device");
+    if (sms_ < 1) sms_ = 1;
+  }
+  // one partial-gradient row per backward CTA (at most one CTA per SM)
+  MLP_TRY(alloc((void**)&Gp_, sizeof(float) * (size_t)NG_STRIDE * sms_), "alloc");
   MLP_TRY(cudaMemsetAsync(M1_, 0, sizeof(float) * NP, stream_), "memset");
   MLP_TRY(cudaMemsetAsync(M2_, 0, sizeof(float) * NP, stream_), "memset");
   MLP_TRY(cudaMemsetAsync(err_, 0, sizeof(int), stream_), "memset");
@@ -618,7 +725,10 @@ std::string Net::check_err() {
 
 std::string Net::forward_dev(const __nv_bfloat16* X, int n, const int* n_dev, int max_n, float* y,
                              __nv_bfloat16* acts, cudaStream_t st) {
-  const int grid = (max_n + TILE - 1) / TILE;
+  // one CTA per SM at most, each over several sample tiles (the weights are
+  // staged once per CTA)
+  const int tiles = (max_n + TILE - 1) / TILE;
+  const int grid = tiles < sms_ ? tiles : sms_;
   if (grid <= 0) return "";
   k_mlp_fwd<<<grid, 128, fwd_smem(), st>>>(X, n, n_dev, Wb_, P_ + 3 * F * F, P_ + 3 * F * F + 3 * F,
                                             P_ + 3 * F * F + 4 * F, y, acts, err_);
@@ -627,11 +737,14 @@ std::string Net::forward_dev(const __nv_bfloat16* X, int n, const int* n_dev, in
 }
 
 std::string Net::backward_dev(const __nv_bfloat16* X, int n, const __nv_bfloat16* acts, const float* y,
-                              const float* t, cudaStream_t st) {
-  const int grid = (n + TILE - 1) / TILE;
+                              const float* t, cudaStream_t st, float* loss_sink) {
+  const int tiles = (n + TILE - 1) / TILE;
+  const int grid = tiles < sms_ ? tiles : sms_;
   if (grid <= 0) return "";
-  k_mlp_bwd<<<grid, 128, bwd_smem(), st>>>(X, n, WTb_, P_ + 3 * F * F + 4 * F - F, acts, y, t, 1.f / n, G_, err_);
+  k_mlp_bwd<<<grid, 128, bwd_smem(), st>>>(X, n, WTb_, P_ + 3 * F * F + 4 * F - F, acts, y, t, 1.f / n, Gp_, err_);
   MLP_TRY(cudaGetLastError(), "mlp backward");
+  k_mlp_reduce<<<(NG + 255) / 256, 256, 0, st>>>(Gp_, grid, G_, loss_sink);
+  MLP_TRY(cudaGetLastError(), "mlp gradient reduction");
   return "";
 }
 
@@ -729,31 +842,31 @@ std::string Net::train_dev_upload(const __nv_bfloat16* xb, const float* th, int 
 std::string Net::train_device(const __nv_bfloat16* X, const float* t, int n, int epochs, int batch, float lr,
                               __nv_bfloat16* Aa, float* y, float* last_loss) {
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  double loss_sum = 0;
+  float loss_sum = 0.f;
   int loss_cnt = 0;
   for (int ep = 0; ep < epochs; ++ep) {
-    loss_sum = 0;
+    // the batches' losses add up on the device; one read per epoch
+    MLP_TRY(cudaMemsetAsync(loss_acc_, 0, sizeof(float), stream_), "memset");
     loss_cnt = 0;
     for (int s0 = 0; s0 < n; s0 += batch) {
       const int m = (n - s0) < batch ? (n - s0) : batch;
-      MLP_TRY(cudaMemsetAsync(G_, 0, sizeof(float) * NG, stream_), "memset");
       const __nv_bfloat16* Xb = X + (size_t)s0 * F;
       std::string r = forward_dev(Xb, m, nullptr, m, y, Aa, stream_);
-      if (r.empty()) r = backward_dev(Xb, m, Aa, y, t + s0, stream_);
+      if (r.empty()) r = backward_dev(Xb, m, Aa, y, t + s0, stream_, loss_acc_);
       if (!r.empty()) return r;
       ++step_;
       const float c1 = 1.f / (1.f - std::pow(b1, (float)step_));
       const float c2 = 1.f / (1.f - std::pow(b2, (float)step_));
       k_adam<<<(NP + 255) / 256, 256, 0, stream_>>>(P_, G_, M1_, M2_, NP, lr, b1, b2, eps, c1, c2, Wb_, WTb_);
       MLP_TRY(cudaGetLastError(), "adam");
-      float l = 0.f;
-      MLP_TRY(cudaMemcpyAsync(&l, G_ + NP, sizeof(float), cudaMemcpyDeviceToHost, stream_), "d2h");
-      MLP_TRY(cudaStreamSynchronize(stream_), "sync");
-      loss_sum += l;
       ++loss_cnt;
     }
+    MLP_TRY(cudaMemcpyAsync(&loss_sum, loss_acc_, sizeof(float), cudaMemcpyDeviceToHost, stream_), "d2h");
+    MLP_TRY(cudaStreamSynchronize(stream_), "sync");
+    std::string r = check_err();
+    if (!r.empty()) return r;
   }
-  if (last_loss) *last_loss = loss_cnt ? (float)(loss_sum / loss_cnt) : 0.f;
+  if (last_loss) *last_loss = loss_cnt ? loss_sum / loss_cnt : 0.f;
   return check_err();
 }
 
@@ -822,6 +935,27 @@ std::string Net::append_pairs(const __nv_bfloat16* X, const float* t, const int*
   MLP_TRY(cudaStreamSynchronize(stream_), "sync");
   if (added) *added = num_pairs() - before;
   return "";
+}
+
+std::string Net::eval_pairs(long long first, long long count, float* abs_err) {
+  const long long n = num_pairs();
+  if (first < 0 || count < 0 || first + count > n) return "pair range outside the buffer";
+  if (count == 0) return "";
+  if (count > 0x7fffffffLL) return "too many pairs";
+  float* y = nullptr;
+  MLP_TRY(cudaMalloc(&y, sizeof(float) * (size_t)count), "alloc");
+  std::string r = forward_dev(PX_ + (size_t)first * F, (int)count, nullptr, (int)count, y, nullptr, stream_);
+  std::vector<float> yh((size_t)count), th((size_t)count);
+  if (r.empty() &&
+      (cudaMemcpyAsync(yh.data(), y, sizeof(float) * (size_t)count, cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
+       cudaMemcpyAsync(th.data(), PT_ + first, sizeof(float) * (size_t)count, cudaMemcpyDeviceToHost, stream_) !=
+           cudaSuccess))
+    r = "d2h";
+  cudaStreamSynchronize(stream_);
+  cudaFree(y);
+  if (!r.empty()) return r;
+  for (long long i = 0; i < count; ++i) abs_err[i] = std::fabs(yh[(size_t)i] - th[(size_t)i]);
+  return check_err();
 }
 
 std::string Net::train_pairs(int epochs, int batch, float lr, unsigned long long seed, float* last_loss) {

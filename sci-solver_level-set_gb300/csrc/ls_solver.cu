@@ -201,6 +201,7 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
     for (int p = 0; p < np; ++p)
       for (int c = L.ele_offsets[p]; c < L.ele_offsets[p + 1]; ++c) copy_scale[c] = mscale[L.patch_mesh[p]];
   }
+  mesh_scale_ = mscale;
   for (long long c = 0; c < full; ++c) {
     const double cs = batch ? copy_scale[c] : scale;
     const int e = L.ele_permute[c];
@@ -624,10 +625,6 @@ std::string Solver::one_step(bool* empty_nb) {
 
 std::string Solver::learn_buffers() {
   if (X_) return "";
-  if (m_.patch_mesh) {
-    status_ = 1;
-    return "the learned warm start takes one mesh, not a batch";
-  }
   const Layout& L = *lay_;
   const int nv = m_.nv, d1 = m_.dim + 1;
   // 1-ring from the element copies (each element once), sorted and unique
@@ -663,6 +660,17 @@ std::string Solver::learn_buffers() {
   LS_TRY(dalloc(A, &lr_.warm, nv), "alloc");
   LS_TRY(dalloc(A, &lr_.target, nv), "alloc");
   LS_TRY(dalloc(A, &X_, (size_t)nv * 128), "alloc");
+  lr_.vinv_h = nullptr;
+  if (m_.patch_mesh) {
+    // a batch: features and targets in units of each vertex's own mesh
+    std::vector<float> vinv(nv, 1.f);
+    for (int p = 0; p < m_.nparts; ++p)
+      for (int v = L.vert_offsets[p]; v < L.vert_offsets[p + 1]; ++v)
+        vinv[v] = (float)(1.0 / mesh_scale_[L.patch_mesh[p]]);
+    const float* d = nullptr;
+    LS_TRY(upload(A, &d, vinv, stream_), "upload");
+    lr_.vinv_h = d;
+  }
   LS_TRY(cudaStreamSynchronize(stream_), "sync");
   return "";
 }
@@ -705,7 +713,7 @@ std::string Solver::learned_step(bool* empty_nb) {
     LS_TRY(cudaMemsetAsync(lr_.cnt, 0, sizeof(int) * 4, stream_), "memset");
     LS_TRY(K_->learn(LEARN_NB_VERTICES, m_, s_, sp_, lr_, nb_prev, 0.f, L_, stream_), "warm set");
     mlp::k_features<<<L_.flat_grid, 256, 0, stream_>>>(0, lr_.vlist, lr_.cnt, adj_off_, adj_, m_.xyz, m_.nv, s_.phi,
-                                                        1.f / sp_.scale, X_);
+                                                        1.f / sp_.scale, lr_.vinv_h, X_);
     LS_TRY(cudaGetLastError(), "features");
     st_.kernel_launches += 2;
     if (warm) {

@@ -149,6 +149,7 @@ class Solver {
   bool build_persistent_graph(std::string* err);
   cudaError_t step_persistent_launches(int use_all);
   bool persistent_ = false;        // the step's FIM loop is one cooperative launch
+  std::vector<double> mesh_scale_;  // FIM length unit of each mesh (one entry for a single mesh)
   void pull_stats();
   bool stats_stale_ = false;  // device counters changed since the last pull_stats
   // event pairs around the launches of profiled steps (cfg_.profile); kind 0

@@ -73,7 +73,7 @@ EXPORTS = [
     "ls_batch_get_layout", "ls_autotune", "ls_mlp_create", "ls_mlp_destroy", "ls_mlp_last_error",
     "ls_mlp_num_params", "ls_mlp_set_params", "ls_mlp_get_params", "ls_mlp_predict", "ls_mlp_gradients",
     "ls_mlp_train", "ls_mlp_reserve_pairs", "ls_mlp_clear_pairs", "ls_mlp_num_pairs", "ls_mlp_train_pairs",
-    "ls_learn_collect", "ls_set_learned", "ls_partition_graph", "ls_edge_cut",
+    "ls_learn_collect", "ls_set_learned", "ls_batch_set_learned", "ls_mlp_eval_pairs", "ls_partition_graph", "ls_edge_cut",
 ]
 
 class TuneTrial(ctypes.Structure):
@@ -139,6 +139,8 @@ def lib():
     L.ls_mlp_train_pairs.argtypes = [P, I, I, ctypes.c_float, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_float)]
     L.ls_learn_collect.argtypes = [P, P, I, ctypes.POINTER(I)]
     L.ls_set_learned.argtypes = [P, P, ctypes.c_double, ctypes.c_double, I]
+    L.ls_batch_set_learned.argtypes = [P, P, ctypes.c_double, ctypes.c_double, I]
+    L.ls_mlp_eval_pairs.argtypes = [P, ctypes.c_longlong, ctypes.c_longlong, V]
     L.ls_batch_create.argtypes = [ctypes.POINTER(P)]
     L.ls_batch_destroy.argtypes = [P]
     L.ls_batch_last_error.argtypes = [P]
@@ -475,6 +477,10 @@ class LevelSetBatch:
     def set_profile(self, on):
         self._check(lib().ls_batch_set_profile(self._b, 1 if on else 0), "batch set_profile")
 
+    def set_learned(self, mlp, margin=0.0, support_tol=0.0, reset_mode=0):
+        self._check(lib().ls_batch_set_learned(self._b, mlp._m if mlp is not None else None, float(margin),
+                                               float(support_tol), int(reset_mode)), "batch set_learned")
+
     def layout_info(self):
         info = np.zeros(10, np.int64)
         self._check(lib().ls_batch_get_layout_info(self._b, _ptr(info)), "batch layout_info")
@@ -565,6 +571,12 @@ class MLP:
         n = ctypes.c_longlong(0)
         self._check(lib().ls_mlp_num_pairs(self._m, ctypes.byref(n)), "mlp num_pairs")
         return n.value
+
+    def eval_pairs(self, first, count):
+        """|prediction - target| / h of the pairs [first, first + count)."""
+        out = np.zeros(int(count), np.float32)
+        self._check(lib().ls_mlp_eval_pairs(self._m, int(first), int(count), _ptr(out)), "mlp eval_pairs")
+        return out
 
     def train_pairs(self, epochs=1, batch=65536, lr=1e-3, seed=0):
         loss = ctypes.c_float(0)

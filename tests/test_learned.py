@@ -66,3 +66,38 @@ def test_trained_network_needs_fewer_corrections(trained):
     print("plain visits %d checks %d | trained visits %d checks %d resets %d moved %d rounds %d | untrained visits %d"
           % (st_p["patch_visits"], st_p["check_visits"], st_t["patch_visits"], st_t["check_visits"],
              st_t["unsupported_resets"], st_t["moved_vertices"], st_t["support_rounds"], st_u["patch_visits"]))
+
+
+def test_batch_warm_start_is_judged_by_plain_fim(trained):
+    # a batch of meshes of different resolution: features and targets in
+    # each mesh's own units; the warm-started batch stays at the plain batch
+    ws = synth.workload_batch(seed=5, nmesh=4, nmin=12, nmax=24)
+    out = []
+    for mlp in (None, trained):
+        b = lsgb300.LevelSetBatch()
+        for w in ws:
+            b.add(lsgb300.from_workload(w, setup=False))
+        b.setup()
+        if mlp is not None:
+            b.set_learned(mlp, margin=0.3)
+        b.solve(4)
+        out.append(([b.phi(i) for i in range(len(ws))], b.stats()))
+        b.close()
+    (ph0, st0), (ph1, st1) = out
+    assert st1["warm_vertices"] > 0 and st1["support_rounds"] > 0
+    for w, a, c in zip(ws, ph1, ph0):
+        err = _band_err(a, c, w)
+        assert err.max() < 1e-2 and np.mean(err < 1e-3) > 0.99, err.max()
+
+
+def test_held_out_error_of_trained_network(trained):
+    # pairs appended after training, from a run the network never saw
+    first = trained.num_pairs()
+    ls = lsgb300.from_workload(synth.workload("c3", n=24, seed=0))
+    ls.learn_collect(trained, 2)
+    n = trained.num_pairs() - first
+    assert n > 0
+    err = trained.eval_pairs(first, n)
+    assert err.shape == (n,) and np.isfinite(err).all()
+    # a trained network predicts the band's signed distance to a fraction of h
+    assert np.median(err) < 0.5, np.median(err)

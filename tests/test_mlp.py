@@ -77,3 +77,22 @@ def test_training_reduces_loss():
     last = m.train(x, t, epochs=30, batch=4096, lr=1e-3)
     _, l1 = m.gradients(x[:4096], t[:4096])
     assert np.isfinite(last) and l1 < 0.2 * l0, (l0, l1, last)
+
+
+@pytest.mark.gpu
+def test_gradients_over_many_tiles_per_cta_match_reference_and_repeat():
+    # more 128-sample tiles than SMs: each backward CTA accumulates several
+    # tiles in tensor memory, the per-CTA rows are summed in a fixed order
+    m = lsgb300.MLP(0)
+    p = mlp_ref.init_params(8)
+    m.set_params(p)
+    x, t = _data(40000, 11)
+    g, loss = m.gradients(x, t)
+    g2, loss2 = m.gradients(x, t)
+    assert np.array_equal(g.view(np.uint32), g2.view(np.uint32)) and loss == loss2
+    gr, lr = mlp_ref.gradients(p, x, t)
+    assert abs(loss - lr) <= 1e-2 * lr + 1e-6
+    for sl in (slice(0, 3 * 128 * 128), slice(3 * 128 * 128, 3 * 128 * 128 + 384), slice(-129, None)):
+        a, b = g[sl], gr[sl]
+        rel = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-12)
+        assert rel < 3e-2, (sl, rel)
