@@ -559,6 +559,14 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
       // the other parity's counter is idle until the next sweep's listing,
       // which starts after the barrier below
       if (tid == 0) s_n[(it & 1) ^ 1] = 0;
+      // nothing listed: this sweep changes nothing, so every later sweep of
+      // the visit has the same inputs and lists nothing either; the visit
+      // ends here, and the convergence test sees no change, as it would
+      // after the remaining empty sweeps (same bits as running them)
+      if (nitems == 0 && it < niter - 1) {
+        for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
+        break;
+      }
       for (int i = tid; i < nitems; i += blockDim.x) {
         const int code = sItem[i];
         const int cc = code >> 2, k = code & 3;
@@ -669,9 +677,31 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
   }
 }
 
+// Local solver of the two-copies-per-thread sweep: the fast build's
+// planar-wave solver with the lower-bound skip (kPairWave), or the
+// reference's solver in its operand order, every listed solve run (the
+// bit-exact build; kPairRefXdiv with the interior division in double, as
+// the reference semantics there).
+constexpr int kPairWave = 0, kPairRef = 1, kPairRefXdiv = 2;
+
+// Can solve k (listed as a candidate: its inputs changed) lower its target
+// T_k?  Not when the three other values are all LARGENUM (the solver returns
+// LARGENUM); with the planar-wave solver also not when min of them plus
+// 0.999 x the target's height over their face is at least T_k (the lower
+// bound of every candidate in exact arithmetic).  The reference solver's
+// FP32 candidates can fall below that bound, so the bit-exact build keeps
+// those solves.
+template <int SOLVER>
+__device__ __forceinline__ bool pair_may_lower(unsigned cand, float mn, float hk, float tk, float LN) {
+  if (!cand || !(mn < LN)) return false;
+  if constexpr (SOLVER == kPairWave) return mn + 0.999f * hk < tk;
+  return true;
+}
+
 // One listed solve of k_fim_pair: solve k of copy cc from the copy values
 // at the sweep start; the result lowers the owned target's shared value or
 // becomes the copy's private ghost value.
+template <int SOLVER>
 __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const float4* sM, const float4* sH,
                                            const ushort4* sC, float* sT, float4* sR, int nvp, const StepParams& sp) {
   const int cc = code >> 2, k = code & 3;
@@ -686,9 +716,16 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
   else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
   else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
   else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
-  const float4 hv = sH[cc];
-  const float hD = k == 0 ? hv.x : k == 1 ? hv.y : k == 2 ? hv.z : hv.w;
-  const float r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, hD, sp.eps_h, sp.largenum);
+  float r;
+  if constexpr (SOLVER == kPairWave) {
+    const float4 hv = sH[cc];
+    const float hD = k == 0 ? hv.x : k == 1 ? hv.y : k == 2 ? hv.z : hv.w;
+    r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, hD, sp.eps_h, sp.largenum);
+  } else {
+    bool d = false;
+    r = tet_solve<float, SOLVER == kPairRefXdiv, false, false>(a0, a1, a2, g0, g1, g2, g3, g4, g5, sp.eps_h,
+                                                                sp.eps_h64, sp.largenum, 0.f, d, own);
+  }
   const float nw = fminf(own, r);
   const ushort4 cv = sC[cc];
   const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
@@ -799,6 +836,7 @@ __device__ __forceinline__ bool slab_wait(unsigned bar, unsigned parity, bool gi
 // that finds its patch unconverged goes on to run that patch's visit (the
 // next iteration's visit would read the same DT) and marks the patch's entry
 // in the next list with kPrevisited; the next sweep skips marked entries.
+template <int SOLVER>
 __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& s, const StepParams& sp, int cur,
                                               int check, int vb) {
   const bool CHECK = check != 0;
@@ -954,10 +992,10 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
             if (chg & 0x7u) cand |= 8u;
             cand &= (~ghost | allow_ghost) & 0xFu;
             unsigned nd = 0u;
-            if ((cand & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
-            if ((cand & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
-            if ((cand & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
-            if ((cand & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
+            if (pair_may_lower<SOLVER>(cand & 1u, m123, hv.x, tv.x, LN)) nd |= 1u;
+            if (pair_may_lower<SOLVER>(cand & 2u, m023, hv.y, tv.y, LN)) nd |= 2u;
+            if (pair_may_lower<SOLVER>(cand & 4u, m013, hv.z, tv.z, LN)) nd |= 4u;
+            if (pair_may_lower<SOLVER>(cand & 8u, m012, hv.w, tv.w, LN)) nd |= 8u;
             need[j] = nd;
           }
         }
@@ -980,7 +1018,14 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
         // the other parity's counter is idle until the next sweep's listing,
         // which starts after the barrier below
         if (tid == 0) s_n[(it & 1) ^ 1] = 0;
-        for (int i = tid; i < nitems; i += blockDim.x) pair_solve(sItem[i], sTc, sM, sH, sC, sT, sR, nvp, sp);
+        // nothing listed in a visit's sweep before its last: no later sweep
+        // lists anything either (unchanged inputs), so the visit ends here
+        // with the bits the remaining empty sweeps would leave
+        if (nitems == 0 && visit && it < niter_p - 1) {
+          for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
+          break;
+        }
+        for (int i = tid; i < nitems; i += blockDim.x) pair_solve<SOLVER>(sItem[i], sTc, sM, sH, sC, sT, sR, nvp, sp);
         __syncthreads();
         if (CHECK && !visit) {
           // the check's verdict (as at the end of a check): does an owned
@@ -1008,10 +1053,10 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
                 const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
                 const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
                 unsigned nd = 0u;
-                if ((ghost & 1u) && m123 < LN && m123 + 0.999f * hv.x < tv.x) nd |= 1u;
-                if ((ghost & 2u) && m023 < LN && m023 + 0.999f * hv.y < tv.y) nd |= 2u;
-                if ((ghost & 4u) && m013 < LN && m013 + 0.999f * hv.z < tv.z) nd |= 4u;
-                if ((ghost & 8u) && m012 < LN && m012 + 0.999f * hv.w < tv.w) nd |= 8u;
+                if (pair_may_lower<SOLVER>(ghost & 1u, m123, hv.x, tv.x, LN)) nd |= 1u;
+                if (pair_may_lower<SOLVER>(ghost & 2u, m023, hv.y, tv.y, LN)) nd |= 2u;
+                if (pair_may_lower<SOLVER>(ghost & 4u, m013, hv.z, tv.z, LN)) nd |= 4u;
+                if (pair_may_lower<SOLVER>(ghost & 8u, m012, hv.w, tv.w, LN)) nd |= 8u;
                 need[j] |= nd;
                 const int n = __popc(nd);
                 if (n) {
@@ -1024,7 +1069,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
             }
             __syncthreads();
             const int ng = s_ng;
-            for (int i = tid; i < ng; i += blockDim.x) pair_solve(sItem[nitems + i], sTc, sM, sH, sC, sT, sR, nvp, sp);
+            for (int i = tid; i < ng; i += blockDim.x) pair_solve<SOLVER>(sItem[nitems + i], sTc, sM, sH, sC, sT, sR, nvp, sp);
             __syncthreads();
           }
         }
@@ -1120,9 +1165,9 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   if (tid == 0 && !in_flight) slab_bar_inval(bar);
 }
 
-template <int MINB>
+template <int MINB, int SOLVER>
 __global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
-  fim_pair_pass(m, s, sp, cur, check, blockIdx.x);
+  fim_pair_pass<SOLVER>(m, s, sp, cur, check, blockIdx.x);
 }
 
 // Schedule of one FIM iteration: one warp per patch of the current list.
@@ -1304,9 +1349,10 @@ __device__ __forceinline__ void fim_loop_persistent(const DevMesh& m, const DevS
   }
 }
 
-template <int MINB>
+template <int MINB, int SOLVER>
 __global__ void __launch_bounds__(192, MINB) k_fim_pair_persist(DevMesh m, DevState s, StepParams sp) {
-  fim_loop_persistent(m, s, sp, [&](int cur, int check, int vb) { fim_pair_pass(m, s, sp, cur, check, vb); });
+  fim_loop_persistent(m, s, sp,
+                      [&](int cur, int check, int vb) { fim_pair_pass<SOLVER>(m, s, sp, cur, check, vb); });
 }
 
 template <int D1, int MAXT, bool XDIV, int MINB, bool PREC>
@@ -1901,6 +1947,37 @@ inline int pair_smem(const StepParams& sp, int ncap) {
   return (int)sizeof(float) * ((2 * sp.lvp + sp.lgp + 3) & ~3) + ncap * (16 * 3 + 48 + 8 + 8 + 1);
 }
 
+// The two-copies-per-thread kernels of this build: the planar-wave solver
+// (fast build) or the reference's solver (bit-exact build; its interior
+// division in double with the reference's semantics).
+#ifdef LS_KERNELS_EXACT
+#define LS_PAIR_SOLVER(sp) ((sp).xdiv ? kPairRefXdiv : kPairRef)
+#define LS_PAIR_KERNEL(sp) ((sp).xdiv ? (const void*)k_fim_pair<5, kPairRefXdiv> : (const void*)k_fim_pair<5, kPairRef>)
+#define LS_PAIR_PERSIST(sp) \
+  ((sp).xdiv ? (const void*)k_fim_pair_persist<5, kPairRefXdiv> : (const void*)k_fim_pair_persist<5, kPairRef>)
+#else
+#define LS_PAIR_KERNEL(sp) ((const void*)k_fim_pair<5, kPairWave>)
+#define LS_PAIR_PERSIST(sp) ((const void*)k_fim_pair_persist<5, kPairWave>)
+#endif
+
+// Tetrahedra without capped corners, no precision form, patches of up to
+// 384 copies, FIM setting 5: the two-copies-per-thread sweep (L.pair_block).
+__host__ __device__ inline bool use_pair(const DevMesh& m, const StepParams& sp, const Launch& L) {
+  return m.dim == 3 && !m.capped && !(sp.tau > 0.f) && L.pair_block > 0;
+}
+
+cudaError_t launch_pair(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, int c, const Launch& L,
+                        cudaStream_t st) {
+  const int smem = pair_smem(sp, sp.lep);
+#ifdef LS_KERNELS_EXACT
+  if (sp.xdiv) k_fim_pair<5, kPairRefXdiv><<<L.fim_grid, L.pair_block, smem, st>>>(m, s, sp, cur, c);
+  else k_fim_pair<5, kPairRef><<<L.fim_grid, L.pair_block, smem, st>>>(m, s, sp, cur, c);
+#else
+  k_fim_pair<5, kPairWave><<<L.fim_grid, L.pair_block, smem, st>>>(m, s, sp, cur, c);
+#endif
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
                          const Launch& L, cudaStream_t st) {
   const bool xd = sp.xdiv != 0;
@@ -1920,16 +1997,16 @@ cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& 
   // semantics only) take the one-copy-per-thread kernel, which keeps those
   // corners private
   const bool compact = kLbSkip && m.dim == 3 && !m.capped;
-  if (compact && pr) {
+  if (use_pair(m, sp, L)) {
+    // tetrahedra: compacted solves, two copies per thread
+    return launch_pair(m, s, sp, cur, c, L, st);
+  } else if (compact && pr) {
     // fast build, tetrahedra, precision form: compacted solves, FP64 repeats
     // run densely after each sweep's FP32 pass
     const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
     if (L.fim_block <= 384) k_fim_compact<384, 2, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     else if (L.fim_block <= 512) k_fim_compact<512, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
     else k_fim_compact<1024, 1, true><<<L.fim_grid, L.fim_block, cs, st>>>(m, s, sp, cur, c);
-  } else if (compact && L.pair_block > 0) {
-    // fast build, tetrahedra: compacted solves, two copies per thread
-    k_fim_pair<5><<<L.fim_grid, L.pair_block, pair_smem(sp, sp.lep), st>>>(m, s, sp, cur, c);
   } else if (compact) {
     // fast build, tetrahedra: compacted solves
     const int cs = compact_smem(sp, L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024);
@@ -1980,10 +2057,15 @@ cudaError_t launch_fim_persistent(const DevMesh& m, const DevState& s, const Ste
   const bool xd = sp.xdiv != 0;
   const bool pr = sp.tau > 0.f;
   const bool compact = kLbSkip && m.dim == 3 && !m.capped;
-  if (compact && !pr && L.pair_block > 0) {
+  if (use_pair(m, sp, L)) {
     cfg.blockDim = dim3((unsigned)L.pair_block);
     cfg.dynamicSmemBytes = (size_t)pair_smem(sp, sp.lep);
-    return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5>, m, s, sp);
+#ifdef LS_KERNELS_EXACT
+    if (sp.xdiv) return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5, kPairRefXdiv>, m, s, sp);
+    return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5, kPairRef>, m, s, sp);
+#else
+    return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5, kPairWave>, m, s, sp);
+#endif
   }
   if (compact || L.fim_block > 384) return cudaErrorNotSupported;
   cfg.blockDim = dim3((unsigned)L.fim_block);
@@ -2013,8 +2095,8 @@ cudaError_t configure_persistent(const DevMesh& m, const StepParams& sp, Launch&
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, smem);
   };
-  if (compact && !pr && L.pair_block > 0) {
-    query((const void*)k_fim_pair_persist<5>, L.pair_block, pair_smem(sp, sp.lep));
+  if (use_pair(m, sp, L)) {
+    query(LS_PAIR_PERSIST(sp), L.pair_block, pair_smem(sp, sp.lep));
   } else if (!compact && L.fim_block <= 384) {
     const int psmem = L.fim_smem + (int)sizeof(DeferredSolve) * kDeferCap;
     const int sm = pr ? psmem : L.fim_smem;
@@ -2094,8 +2176,9 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
       // two copies per thread: ceil(lep / 2) threads, whole warps
       L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;
       const int ps = pair_smem(sp, sp.lep);
-      e = cudaFuncSetAttribute(k_fim_pair<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
-      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_pair<5>, L.pair_block, ps);
+      e = cudaFuncSetAttribute(LS_PAIR_KERNEL(sp), cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, LS_PAIR_KERNEL(sp), L.pair_block, ps);
     } else if (L.fim_block <= 384 && sp.ctas == 2) {
       e = cudaFuncSetAttribute(k_fim_compact<384, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
       if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim_compact<384, 2, false>, L.fim_block, cs);
@@ -2122,7 +2205,15 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
         e = cudaFuncSetAttribute(k_fim_compact<1024, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     }
   } else if (m.dim == 3) {
-    if (L.fim_block <= 384 && sp.ctas == 2)
+    if (!m.capped && L.fim_block <= 384 && sp.ctas == 5) {
+      // bit-exact build: two copies per thread with the reference's solver
+      // (the precision form keeps the one-copy kernel)
+      L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;
+      const int ps = pair_smem(sp, sp.lep);
+      e = cudaFuncSetAttribute(LS_PAIR_KERNEL(sp), cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, LS_PAIR_KERNEL(sp), L.pair_block, ps);
+    } else if (L.fim_block <= 384 && sp.ctas == 2)
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 2, false>, L.fim_block, L.fim_smem);
     else if (L.fim_block <= 384 && sp.ctas == 4)
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fim<4, 384, false, 4, false>, L.fim_block, L.fim_smem);
