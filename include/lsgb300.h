@@ -112,7 +112,8 @@ typedef struct ls_params {
   double fp64_threshold;  /* LS_FP64_FLAGGED: discriminant cancellation threshold tau (0 -> 2^-18) */
   int graph_chunk;        /* FIM iterations per loop body of the step graph (0 -> 4, rounded up to even) */
   int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 with one element copy
-                             per thread; 5: two copies per thread (fast build, tetrahedra; others run 3)
+                             per thread; 5 or 6: two copies per thread, five CTAs per SM (64 registers) or
+                             six (56 registers) (tetrahedra without the precision form; others run 3)
                              (0 -> 5) */
   int barrier_wait_limit; /* LS_PERSISTENT: polls (about 0.25 us apart) one grid-barrier wait may take
                              before the step is abandoned with LS_DEVICE_TIMEOUT (0 -> 4194304, about a

@@ -520,10 +520,10 @@ __global__ void __launch_bounds__(MAXT, MINB) k_fim_compact(DevMesh m, DevState 
     }
 #pragma unroll 1
     for (int it = 0; it < niter; ++it) {
-      if (it == niter - 1) {
+      // the owned values at the start of the last sweep (read back by the
+      // same thread only; the solves change sT after the listing barrier)
+      if (it == niter - 1)
         for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
-        __syncthreads();
-      }
       // list the solves that can lower their target
       unsigned need = 0;
       if (act) {
@@ -964,10 +964,11 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       unsigned need[2] = {0u, 0u};
   #pragma unroll 1
       for (int it = 0; it < niter_p; ++it) {
-        if (it == niter_p - 1) {
+        // the owned values at the start of the last sweep (read back by the
+        // same thread only; this sweep's solves change sT only after the
+        // listing barrier below, so no barrier of its own)
+        if (it == niter_p - 1)
           for (int i = tid; i < nvp; i += blockDim.x) sOld[i] = sT[i];
-          __syncthreads();
-        }
         // list this thread's solves that can lower their target (the tests of
         // k_fim_compact)
         const unsigned allow_ghost = (it == niter_p - 1) ? 0u : 0xFu;
@@ -1950,15 +1951,16 @@ inline int pair_smem(const StepParams& sp, int ncap) {
 // The two-copies-per-thread kernels of this build: the planar-wave solver
 // (fast build) or the reference's solver (bit-exact build; its interior
 // division in double with the reference's semantics).
+// Setting 5: five CTAs per SM (64 registers); setting 6: six (56 registers).
 #ifdef LS_KERNELS_EXACT
-#define LS_PAIR_SOLVER(sp) ((sp).xdiv ? kPairRefXdiv : kPairRef)
-#define LS_PAIR_KERNEL(sp) ((sp).xdiv ? (const void*)k_fim_pair<5, kPairRefXdiv> : (const void*)k_fim_pair<5, kPairRef>)
-#define LS_PAIR_PERSIST(sp) \
-  ((sp).xdiv ? (const void*)k_fim_pair_persist<5, kPairRefXdiv> : (const void*)k_fim_pair_persist<5, kPairRef>)
+#define LS_PAIR_PICK(K, sp)                                                                         \
+  ((sp).ctas == 6 ? ((sp).xdiv ? (const void*)K<6, kPairRefXdiv> : (const void*)K<6, kPairRef>) \
+                  : ((sp).xdiv ? (const void*)K<5, kPairRefXdiv> : (const void*)K<5, kPairRef>))
 #else
-#define LS_PAIR_KERNEL(sp) ((const void*)k_fim_pair<5, kPairWave>)
-#define LS_PAIR_PERSIST(sp) ((const void*)k_fim_pair_persist<5, kPairWave>)
+#define LS_PAIR_PICK(K, sp) ((sp).ctas == 6 ? (const void*)K<6, kPairWave> : (const void*)K<5, kPairWave>)
 #endif
+#define LS_PAIR_KERNEL(sp) LS_PAIR_PICK(k_fim_pair, sp)
+#define LS_PAIR_PERSIST(sp) LS_PAIR_PICK(k_fim_pair_persist, sp)
 
 // Tetrahedra without capped corners, no precision form, patches of up to
 // 384 copies, FIM setting 5: the two-copies-per-thread sweep (L.pair_block).
@@ -1968,14 +1970,9 @@ __host__ __device__ inline bool use_pair(const DevMesh& m, const StepParams& sp,
 
 cudaError_t launch_pair(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, int c, const Launch& L,
                         cudaStream_t st) {
-  const int smem = pair_smem(sp, sp.lep);
-#ifdef LS_KERNELS_EXACT
-  if (sp.xdiv) k_fim_pair<5, kPairRefXdiv><<<L.fim_grid, L.pair_block, smem, st>>>(m, s, sp, cur, c);
-  else k_fim_pair<5, kPairRef><<<L.fim_grid, L.pair_block, smem, st>>>(m, s, sp, cur, c);
-#else
-  k_fim_pair<5, kPairWave><<<L.fim_grid, L.pair_block, smem, st>>>(m, s, sp, cur, c);
-#endif
-  return cudaGetLastError();
+  void* args[] = {(void*)&m, (void*)&s, (void*)&sp, (void*)&cur, (void*)&c};
+  return cudaLaunchKernel(LS_PAIR_KERNEL(sp), dim3((unsigned)L.fim_grid), dim3((unsigned)L.pair_block), args,
+                          (size_t)pair_smem(sp, sp.lep), st);
 }
 
 cudaError_t launch_sweep(const DevMesh& m, const DevState& s, const StepParams& sp, int cur, bool check,
@@ -2060,12 +2057,8 @@ cudaError_t launch_fim_persistent(const DevMesh& m, const DevState& s, const Ste
   if (use_pair(m, sp, L)) {
     cfg.blockDim = dim3((unsigned)L.pair_block);
     cfg.dynamicSmemBytes = (size_t)pair_smem(sp, sp.lep);
-#ifdef LS_KERNELS_EXACT
-    if (sp.xdiv) return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5, kPairRefXdiv>, m, s, sp);
-    return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5, kPairRef>, m, s, sp);
-#else
-    return cudaLaunchKernelEx(&cfg, k_fim_pair_persist<5, kPairWave>, m, s, sp);
-#endif
+    void* args[] = {(void*)&m, (void*)&s, (void*)&sp};
+    return cudaLaunchKernelExC(&cfg, LS_PAIR_PERSIST(sp), args);
   }
   if (compact || L.fim_block > 384) return cudaErrorNotSupported;
   cfg.blockDim = dim3((unsigned)L.fim_block);
@@ -2172,7 +2165,7 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
     // grid by its occupancy
     const int maxt = L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024;
     const int cs = compact_smem(sp, maxt);
-    if (L.fim_block <= 384 && sp.ctas == 5) {
+    if (L.fim_block <= 384 && (sp.ctas == 5 || sp.ctas == 6)) {
       // two copies per thread: ceil(lep / 2) threads, whole warps
       L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;
       const int ps = pair_smem(sp, sp.lep);
@@ -2205,7 +2198,7 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
         e = cudaFuncSetAttribute(k_fim_compact<1024, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     }
   } else if (m.dim == 3) {
-    if (!m.capped && L.fim_block <= 384 && sp.ctas == 5) {
+    if (!m.capped && L.fim_block <= 384 && (sp.ctas == 5 || sp.ctas == 6)) {
       // bit-exact build: two copies per thread with the reference's solver
       // (the precision form keeps the one-copy kernel)
       L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;

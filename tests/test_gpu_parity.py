@@ -61,6 +61,26 @@ def test_bitexact_build_equals_oracle(name, n, ref_compat, fp64):
         assert st[k] == ost[k], k
 
 
+@pytest.mark.parametrize("name,n", CASES)
+@pytest.mark.parametrize("ref_compat", [False, True])
+@pytest.mark.parametrize("ctas", [3, 6])
+def test_bitexact_build_other_sweep_settings_equal_oracle(name, n, ref_compat, ctas):
+    # the default setting (5) runs tetrahedra on the two-copies sweep with the
+    # reference's solver; 3 keeps the one-copy kernel that runs every solve,
+    # 6 the two-copies kernel at six CTAs per SM: all equal the oracle
+    w = synth.workload(name, n=n)
+    nsteps = 4
+    ls = lsgb300.from_workload(w, ref_compat=ref_compat, bit_exact=True, fim_ctas_per_sm=ctas)
+    hist, done = ls.solve(nsteps)
+    st = ls.stats()
+    ref, nbs, iters, ost = _oracle(w, ref_compat, 0.0, nsteps)
+    assert done == ost["steps_run"] == nsteps
+    assert np.array_equal(hist.view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(ls.narrowband(w["nparts"]), nbs[-1])
+    for k in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
+        assert st[k] == ost[k], k
+
+
 def _repartition(w, n, kind, size):
     w = dict(w)
     if kind == "block":
@@ -136,17 +156,19 @@ def test_two_copies_per_thread_sweep_equals_one_copy_sweep(name, n, update):
     w = synth.workload(name, n=n)
     if update:
         w["update"] = update
+    # (6: the same kernel at six CTAs per SM)
     nsteps = 4
     runs = []
-    for ctas in (3, 5):
+    for ctas in (3, 5, 6):
         ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
         hist, done = ls.solve(nsteps)
         runs.append((hist, done, ls.stats()))
-    (h3, d3, s3), (h5, d5, s5) = runs
-    assert d3 == d5 == nsteps
-    assert np.array_equal(h3, h5)
-    for key in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
-        assert s3[key] == s5[key], key
+    h3, d3, s3 = runs[0]
+    for h5, d5, s5 in runs[1:]:
+        assert d3 == d5 == nsteps
+        assert np.array_equal(h3, h5)
+        for key in ("fim_iters", "patch_visits", "check_visits", "nb_vertex_updates"):
+            assert s3[key] == s5[key], key
 
 
 def test_visits_run_by_checks_change_nothing():
