@@ -776,20 +776,28 @@ __device__ __forceinline__ void slab_bar_inval(unsigned bar) {
   asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+// The geometry records stream through L2 (about 1.6 GB at 128^3, each read
+// once or twice per step): the copies carry an evict-first L2 policy so that
+// the small arrays on a patch visit's dependent-load chain (list entries,
+// patch offsets, ghost ids, DT) stay in L2.
 __device__ __forceinline__ void geo_issue(const DevMesh& m, int es, int nep, float4* sM, float4* sH, unsigned bar) {
   const unsigned bm = 48u * (unsigned)nep, bh = 16u * (unsigned)nep;
   asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(bar),
                "r"(bm + bh)
                : "memory");
   if (nep > 0) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32addr(sM)),
-                 "l"(__cvta_generic_to_global(m.geo_m + 3ll * es)), "r"(bm), "r"(bar)
-                 : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32addr(sH)),
-                 "l"(__cvta_generic_to_global(m.geo_h + es)), "r"(bh), "r"(bar)
-                 : "memory");
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_u32addr(sM)),
+        "l"(__cvta_generic_to_global(m.geo_m + 3ll * es)), "r"(bm), "r"(bar), "l"(pol)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_u32addr(sH)),
+        "l"(__cvta_generic_to_global(m.geo_h + es)), "r"(bh), "r"(bar), "l"(pol)
+        : "memory");
   }
 }
 
@@ -923,7 +931,8 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         if (c < nep) {
-          const ushort4 cv = m.conn[es + c];
+          // streamed, like the geometry records (evict-first)
+          const ushort4 cv = __ldcs(m.conn + es + c);
           sC[c] = cv;
           const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
                                  (cv.w >= nvp ? 8u : 0u);
