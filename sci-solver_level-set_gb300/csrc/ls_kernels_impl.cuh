@@ -915,24 +915,38 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       // and connectivity load (the previous patch's last reads of sM and sH
       // came before its final barrier)
       if (tid == 0) geo_issue(m, es, nep, sM, sH, bar);
-      for (int i = tid; i < nvp + ngp; i += blockDim.x)
+      // every load of the patch's own slab is issued before any of them is
+      // stored (values, seed flags, connectivity: independent round trips
+      // that overlap; a ghost value waits only for its id), then stored.
+      // First slab entry, seed flag and copies of each thread:
+      const int nslab = nvp + ngp;
+      const int gv0 = tid < nvp ? vs + tid : (tid < nslab ? __ldg(m.ghost_ids + gs + tid - nvp) : -1);
+      const bool sd0 = seed_mask && tid < nvp && s.seed[vs + tid] != 0;
+      ushort4 cvv[2];
+  #pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int c = tid + j * blockDim.x;
+        if (c < nep) cvv[j] = __ldcs(m.conn + es + c);  // streamed, like the geometry records (evict-first)
+      }
+      const float dt0 = gv0 >= 0 ? s.DT[gv0] : 0.f;
+      if (tid < nslab) sT[tid] = dt0;
+      for (int i = tid + blockDim.x; i < nslab; i += blockDim.x)
         sT[i] = s.DT[i < nvp ? vs + i : __ldg(m.ghost_ids + gs + i - nvp)];
       // whole warps run each 32-vertex word (the block is whole warps and the
       // bound a multiple of 32)
       if (seed_mask)
         for (int i = tid; i < ((nvp + 31) & ~31); i += blockDim.x) {
-          const unsigned b = __ballot_sync(0xffffffffu, i < nvp && s.seed[vs + i] != 0);
+          const bool sd = i == tid ? sd0 : (i < nvp && s.seed[vs + i] != 0);
+          const unsigned b = __ballot_sync(0xffffffffu, sd);
           if ((i & 31) == 0) s_seed[i >> 5] = b;
         }
-      // the copies' connectivity and flags do not depend on the values, so
-      // their loads overlap the value gathers above (the previous patch's
-      // last reads of these arrays came before its final barrier)
+      // the copies' connectivity and flags (the previous patch's last reads
+      // of these arrays came before its final barrier)
   #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         if (c < nep) {
-          // streamed, like the geometry records (evict-first)
-          const ushort4 cv = __ldcs(m.conn + es + c);
+          const ushort4 cv = cvv[j];
           sC[c] = cv;
           const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
                                  (cv.w >= nvp ? 8u : 0u);
