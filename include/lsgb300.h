@@ -113,8 +113,9 @@ typedef struct ls_params {
   int graph_chunk;        /* FIM iterations per loop body of the step graph (0 -> 4, rounded up to even) */
   int fim_ctas_per_sm;    /* FIM CTAs per SM for patches of <= 384 copies: 2, 3 or 4 with one element copy
                              per thread; 5 or 6: two copies per thread, five CTAs per SM (64 registers) or
-                             six (56 registers) (tetrahedra without the precision form; others run 3)
-                             (0 -> 5) */
+                             six (56 registers); 7: the same kernel with one copy per thread, three CTAs
+                             per SM (shorter visits when the lists are short) (tetrahedra without the
+                             precision form; others run 3) (0 -> 5) */
   int barrier_wait_limit; /* LS_PERSISTENT: polls (about 0.25 us apart) one grid-barrier wait may take
                              before the step is abandoned with LS_DEVICE_TIMEOUT (0 -> 4194304, about a
                              second).  The FIM kernel's wait for its geometry slab copies is bounded by

@@ -508,8 +508,9 @@ ls_status ls_autotune(ls_handle* h, int trial_steps, ls_tune_report* rep) {
   if (h->user_partition) sizes.push_back(0);
   else if (structured) sizes = (h->is_tri ? std::vector<int>{4, 5, 6, 8} : std::vector<int>{2, 3, 4});
   else sizes = (h->is_tri ? std::vector<int>{16, 25, 36, 64} : std::vector<int>{8, 16, 27, 32, 64});
-  // 2-4: one element copy per thread; 5, 6: two per thread (tetrahedra only)
-  const std::vector<int> ctas = h->is_tri ? std::vector<int>{2, 3, 4} : std::vector<int>{2, 3, 4, 5, 6};
+  // 2-4: one element copy per thread; 5, 6: two per thread; 7: the
+  // two-copies kernel with one copy per thread (tetrahedra only)
+  const std::vector<int> ctas = h->is_tri ? std::vector<int>{2, 3, 4} : std::vector<int>{2, 3, 4, 5, 6, 7};
   const ls_params saved = h->prm;
   struct Trial { int size, ctas; double ms, rate; };
   std::vector<Trial> trials;

@@ -1189,8 +1189,17 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   if (tid == 0 && !in_flight) slab_bar_inval(bar);
 }
 
-template <int MINB, int SOLVER>
-__global__ void __launch_bounds__(192, MINB) k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
+// FIM settings of the two-copies-per-thread sweep: 5 and 6 run blocks of up
+// to 192 threads (two copies each) at five or six CTAs per SM; 7 runs blocks
+// of up to 384 threads, one copy each (the same kernel: copy c of a patch is
+// thread c mod blockDim), at three CTAs per SM -- shorter visits for lists
+// of few patches per SM.
+__host__ __device__ constexpr int pair_maxt(int setting) { return setting == 7 ? 384 : 192; }
+__host__ __device__ constexpr int pair_minb(int setting) { return setting == 7 ? 3 : setting; }
+
+template <int SETTING, int SOLVER>
+__global__ void __launch_bounds__(pair_maxt(SETTING), pair_minb(SETTING))
+    k_fim_pair(DevMesh m, DevState s, StepParams sp, int cur, int check) {
   fim_pair_pass<SOLVER>(m, s, sp, cur, check, blockIdx.x);
 }
 
@@ -1373,8 +1382,9 @@ __device__ __forceinline__ void fim_loop_persistent(const DevMesh& m, const DevS
   }
 }
 
-template <int MINB, int SOLVER>
-__global__ void __launch_bounds__(192, MINB) k_fim_pair_persist(DevMesh m, DevState s, StepParams sp) {
+template <int SETTING, int SOLVER>
+__global__ void __launch_bounds__(pair_maxt(SETTING), pair_minb(SETTING))
+    k_fim_pair_persist(DevMesh m, DevState s, StepParams sp) {
   fim_loop_persistent(m, s, sp,
                       [&](int cur, int check, int vb) { fim_pair_pass<SOLVER>(m, s, sp, cur, check, vb); });
 }
@@ -1976,12 +1986,14 @@ inline int pair_smem(const StepParams& sp, int ncap) {
 // division in double with the reference's semantics).
 // Setting 5: five CTAs per SM (64 registers); setting 6: six (56 registers).
 #ifdef LS_KERNELS_EXACT
-#define LS_PAIR_PICK(K, sp)                                                                         \
-  ((sp).ctas == 6 ? ((sp).xdiv ? (const void*)K<6, kPairRefXdiv> : (const void*)K<6, kPairRef>) \
-                  : ((sp).xdiv ? (const void*)K<5, kPairRefXdiv> : (const void*)K<5, kPairRef>))
+#define LS_PAIR_SOLVERS(K, n, sp) ((sp).xdiv ? (const void*)K<n, kPairRefXdiv> : (const void*)K<n, kPairRef>)
 #else
-#define LS_PAIR_PICK(K, sp) ((sp).ctas == 6 ? (const void*)K<6, kPairWave> : (const void*)K<5, kPairWave>)
+#define LS_PAIR_SOLVERS(K, n, sp) ((const void*)K<n, kPairWave>)
 #endif
+#define LS_PAIR_PICK(K, sp)                                            \
+  ((sp).ctas == 7   ? LS_PAIR_SOLVERS(K, 7, sp)                      \
+   : (sp).ctas == 6 ? LS_PAIR_SOLVERS(K, 6, sp)                      \
+                    : LS_PAIR_SOLVERS(K, 5, sp))
 #define LS_PAIR_KERNEL(sp) LS_PAIR_PICK(k_fim_pair, sp)
 #define LS_PAIR_PERSIST(sp) LS_PAIR_PICK(k_fim_pair_persist, sp)
 
@@ -2188,9 +2200,10 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
     // grid by its occupancy
     const int maxt = L.fim_block <= 384 ? 384 : L.fim_block <= 512 ? 512 : 1024;
     const int cs = compact_smem(sp, maxt);
-    if (L.fim_block <= 384 && (sp.ctas == 5 || sp.ctas == 6)) {
-      // two copies per thread: ceil(lep / 2) threads, whole warps
-      L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;
+    if (L.fim_block <= 384 && sp.ctas >= 5 && sp.ctas <= 7) {
+      // two copies per thread: ceil(lep / 2) threads, whole warps (setting
+      // 7: one copy per thread, lep threads)
+      L.pair_block = sp.ctas == 7 ? L.fim_block : ((sp.lep + 1) / 2 + 31) / 32 * 32;
       const int ps = pair_smem(sp, sp.lep);
       e = cudaFuncSetAttribute(LS_PAIR_KERNEL(sp), cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
       if (e == cudaSuccess)
@@ -2221,10 +2234,10 @@ cudaError_t configure_launch(const DevMesh& m, const StepParams& sp, Launch& L) 
         e = cudaFuncSetAttribute(k_fim_compact<1024, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
     }
   } else if (m.dim == 3) {
-    if (!m.capped && L.fim_block <= 384 && (sp.ctas == 5 || sp.ctas == 6)) {
+    if (!m.capped && L.fim_block <= 384 && sp.ctas >= 5 && sp.ctas <= 7) {
       // bit-exact build: two copies per thread with the reference's solver
       // (the precision form keeps the one-copy kernel)
-      L.pair_block = ((sp.lep + 1) / 2 + 31) / 32 * 32;
+      L.pair_block = sp.ctas == 7 ? L.fim_block : ((sp.lep + 1) / 2 + 31) / 32 * 32;
       const int ps = pair_smem(sp, sp.lep);
       e = cudaFuncSetAttribute(LS_PAIR_KERNEL(sp), cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
       if (e == cudaSuccess)

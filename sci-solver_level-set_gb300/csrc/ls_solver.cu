@@ -303,7 +303,7 @@ std::string Solver::init(const Layout& L, const SolverConfig& cfg, const float* 
   sp_.scale = (float)scale;
   sp_.tau = (cfg.fp64_flagged && L.dim == 3) ? (float)cfg.fp64_tau : 0.f;
   sp_.xdiv = (cfg.bit_exact && ref) ? 1 : 0;
-  sp_.ctas = (cfg.fim_ctas >= 2 && cfg.fim_ctas <= 6) ? cfg.fim_ctas : 5;
+  sp_.ctas = (cfg.fim_ctas >= 2 && cfg.fim_ctas <= 7) ? cfg.fim_ctas : 5;
   sp_.tol = (float)cfg.smallnum;
   sp_.eps_h64 = cfg.smallnum;
   sp_.eps_h = (float)sp_.eps_h64;

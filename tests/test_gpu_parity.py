@@ -63,11 +63,12 @@ def test_bitexact_build_equals_oracle(name, n, ref_compat, fp64):
 
 @pytest.mark.parametrize("name,n", CASES)
 @pytest.mark.parametrize("ref_compat", [False, True])
-@pytest.mark.parametrize("ctas", [3, 6])
+@pytest.mark.parametrize("ctas", [3, 6, 7])
 def test_bitexact_build_other_sweep_settings_equal_oracle(name, n, ref_compat, ctas):
     # the default setting (5) runs tetrahedra on the two-copies sweep with the
     # reference's solver; 3 keeps the one-copy kernel that runs every solve,
-    # 6 the two-copies kernel at six CTAs per SM: all equal the oracle
+    # 6 the two-copies kernel at six CTAs per SM, 7 the same kernel with one
+    # copy per thread: all equal the oracle
     w = synth.workload(name, n=n)
     nsteps = 4
     ls = lsgb300.from_workload(w, ref_compat=ref_compat, bit_exact=True, fim_ctas_per_sm=ctas)
@@ -156,10 +157,10 @@ def test_two_copies_per_thread_sweep_equals_one_copy_sweep(name, n, update):
     w = synth.workload(name, n=n)
     if update:
         w["update"] = update
-    # (6: the same kernel at six CTAs per SM)
+    # (6: the same kernel at six CTAs per SM; 7: with one copy per thread)
     nsteps = 4
     runs = []
-    for ctas in (3, 5, 6):
+    for ctas in (3, 5, 6, 7):
         ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
         hist, done = ls.solve(nsteps)
         runs.append((hist, done, ls.stats()))
