@@ -619,7 +619,7 @@ def main():
                 # the FIM kernel is bound by instruction issue of the local
                 # solvers, not by HBM: issue slots active from the committed
                 # ncu capture of its sweep and check launches
-                "limiter": "SM instruction issue (FP32/ALU/MUFU of the local solvers); DRAM at 3-6 % of peak",
+                "limiter": "SM instruction issue (FP32/ALU/MUFU of the local solvers); DRAM at 4-13 % of peak",
                 "issue_slots_active": profile_value("issue_slots_active")}
 
     cpu = None
