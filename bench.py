@@ -267,10 +267,22 @@ def run_batched(args, rank, world, local):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     net, training = (train_network(args.n) if args.learned else (None, None))
 
+    # patch side and FIM setting tuned over the whole batch (2 timed steps per
+    # candidate); the timed batches use the pick
+    tb = lsgb300.LevelSetBatch()
+    for w in ws:
+        tb.add(lsgb300.from_workload(w, setup=False, structured_block=3))
+    trials, best = tb.autotune(2)
+    tb.close()
+    pick = trials[best]
+    tune = {"patch_side_vertices": pick["patch_size"], "fim_ctas_per_sm": pick["fim_ctas_per_sm"],
+            "trials": [[t["patch_size"], t["fim_ctas_per_sm"], round(t["ms_per_step"], 3)] for t in trials]}
+
     def run_batch(learned):
         b = lsgb300.LevelSetBatch()
         for w in ws:
-            b.add(lsgb300.from_workload(w, setup=False))
+            b.add(lsgb300.from_workload(w, setup=False, structured_block=pick["patch_size"],
+                                        fim_ctas_per_sm=pick["fim_ctas_per_sm"]))
         b.setup()
         if learned:
             b.set_learned(net, margin=0.3, reset_mode=0)
@@ -314,7 +326,7 @@ def run_batched(args, rank, world, local):
     # the same meshes one handle at a time (the reference's one-mesh-per-solver use)
     seq_ms, seq_updates = 0.0, 0
     for w in ws:
-        ls = lsgb300.from_workload(w)
+        ls = lsgb300.from_workload(w, structured_block=pick["patch_size"], fim_ctas_per_sm=pick["fim_ctas_per_sm"])
         for _ in range(args.warmup):
             ls.step(1)
         ls.reset_stats()
@@ -330,8 +342,8 @@ def run_batched(args, rank, world, local):
         "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded jittered cubes, 1-3 sphere unions, random rigid rotations)",
-        "config": {"workload": "c5 batch of %d meshes (%d verts, %d tets), w=5h, CFL 0.5, 3x3x3-vertex patches"
-                               % (len(ws), nv, ne),
+        "config": {"workload": "c5 batch of %d meshes (%d verts, %d tets), w=5h, CFL 0.5" % (len(ws), nv, ne),
+                   "autotune": tune,
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "single GPU",
                    "fim_iters_per_step": st["fim_iters"] / args.steps,
                    "patch_visits_per_step": st["patch_visits"] / args.steps,

@@ -308,8 +308,9 @@ ls_status ls_edge_cut(int dim, const int* elems, int ne, int nv, const int* npar
  * partition_type = 1, patch target size (metis_size) 8, 16, 27, 32, 64 (3D)
  * / 16, 25, 36, 64 (2D) for the graph and RCB partitioners, or only the
  * caller's partition when ls_set_partition was
- * used -- and each FIM CTAs-per-SM setting (2, 3, 4; patches of up to 384
- * element copies), picks the highest narrowband vertex-updates/s, writes it
+ * used -- and each FIM setting of fim_ctas_per_sm (2-4; tetrahedra also 5-7;
+ * patches of up to 384 element copies), picks the highest narrowband
+ * vertex-updates/s, writes it
  * into the handle's parameters (block_size or metis_size,
  * fim_ctas_per_sm) and leaves the handle set up at phi0 with it. */
 #define LS_TUNE_MAX_TRIALS 32
@@ -348,6 +349,15 @@ const char* ls_batch_last_error(ls_batch* b);
 ls_status ls_batch_add(ls_batch* b, ls_handle* h, int* index);
 ls_status ls_batch_setup(ls_batch* b);
 ls_status ls_batch_solve(ls_batch* b, int nsteps, int* steps_done);
+/* Autotuner of a batch (no counterpart in the reference): as ls_autotune,
+ * over the whole batch -- each member laid out again with each candidate
+ * patch size (when every member uses the library's partitioner of one
+ * type; a caller's partition is kept), each FIM setting timed on the merged
+ * patch set for trial_steps steps after one warm-up step -- and leaves the
+ * batch set up with the best, every member at its phi0.  Replaces the
+ * batch's solver (call it before ls_batch_solve, or ls_batch_setup again
+ * after it). */
+ls_status ls_batch_autotune(ls_batch* b, int trial_steps, ls_tune_report* rep);
 /* phi of one member, in that member's vertex order */
 ls_status ls_batch_get_phi(ls_batch* b, int index, float* phi);
 ls_status ls_batch_get_stats(ls_batch* b, ls_stats* s);

@@ -43,6 +43,13 @@ struct ls_batch {
     std::vector<float> phi, vel;
     ls_params prm;
     int nv = 0, ne = 0;
+    // the member's mesh and partition inputs, kept so that the batch
+    // autotuner can lay the member out again with another patch size
+    std::vector<float> xyz;
+    std::vector<int> elems;
+    std::vector<int> npart;  // the caller's partition (user_partition)
+    int nparts = 0;
+    bool user_partition = false;
   };
   std::vector<Member> members;
   int is_tri = -1;
@@ -652,6 +659,13 @@ ls_status ls_batch_add(ls_batch* b, ls_handle* h, int* index) {
   m.prm = h->prm;
   m.nv = h->nv;
   m.ne = h->ne;
+  m.xyz = h->xyz;
+  m.elems = h->elems;
+  m.user_partition = h->user_partition;
+  if (h->user_partition) {
+    m.npart = h->npart;
+    m.nparts = h->nparts;
+  }
   b->members.push_back(std::move(m));
   if (index) *index = (int)b->members.size() - 1;
   return LS_OK;
@@ -690,6 +704,124 @@ ls_status ls_batch_setup(ls_batch* b) {
   }
   b->stage.assign(vb, 0.f);
   return bsolver_status(b, b->solver->set_phi(phi.data()));
+}
+
+namespace {
+// Lays member m out again with patch size `size` (block side or partition
+// target, by its partition type) through a temporary handle.
+ls_status relayout_member(ls_batch* b, ls_batch::Member& m, int size) {
+  ls_handle t;
+  t.is_tri = b->is_tri;
+  t.prm = m.prm;
+  if (t.prm.partition_type == 1) t.prm.block_size = size;
+  else t.prm.metis_size = size;
+  t.xyz = m.xyz;
+  t.elems = m.elems;
+  t.nv = m.nv;
+  t.ne = m.ne;
+  t.phi = m.phi;
+  t.vel = m.vel;
+  t.have_phi = t.have_vel = true;
+  ls_status s = ls_prepare(&t);
+  if (s != LS_OK) return bfail(b, s, "member layout: " + t.err);
+  m.layout = *t.layout;
+  m.prm = t.prm;
+  return LS_OK;
+}
+}  // namespace
+
+ls_status ls_batch_autotune(ls_batch* b, int trial_steps, ls_tune_report* rep) {
+  if (!b) return LS_BAD_INPUT;
+  if (b->members.empty()) return bfail(b, LS_BAD_INPUT, "empty batch");
+  if (trial_steps <= 0) trial_steps = 2;
+  // patch sizes: only when every member is partitioned by the library with
+  // the same partition type (a caller's partition is kept as it is)
+  const int ptype = b->members[0].prm.partition_type;
+  bool tunable = true;
+  for (auto& m : b->members) tunable &= !m.user_partition && m.prm.partition_type == ptype;
+  std::vector<int> sizes;
+  if (!tunable) sizes.push_back(0);
+  else if (ptype == 1) sizes = b->is_tri ? std::vector<int>{4, 5, 6, 8} : std::vector<int>{2, 3, 4};
+  else sizes = b->is_tri ? std::vector<int>{16, 25, 36, 64} : std::vector<int>{8, 16, 27, 32, 64};
+  const std::vector<int> ctas = b->is_tri ? std::vector<int>{2, 3, 4} : std::vector<int>{2, 3, 4, 5, 6, 7};
+  std::vector<ls_params> saved;
+  std::vector<lsgb::Layout> saved_layouts;
+  for (auto& m : b->members) {
+    saved.push_back(m.prm);
+    saved_layouts.push_back(m.layout);
+  }
+  auto restore = [&] {
+    for (size_t i = 0; i < b->members.size(); ++i) {
+      b->members[i].prm = saved[i];
+      b->members[i].layout = saved_layouts[i];
+    }
+  };
+  struct Trial { int size, ctas; double ms, rate; };
+  std::vector<Trial> trials;
+  for (int sz : sizes) {
+    b->solver.reset();
+    bool fits = true;
+    for (auto& m : b->members) {
+      ls_status s = sz > 0 ? relayout_member(b, m, sz) : LS_OK;
+      if (s == LS_PATCH_TOO_LARGE) { fits = false; break; }
+      if (s != LS_OK) { restore(); return s; }
+    }
+    if (!fits) continue;
+    int lep = 0;
+    for (auto& m : b->members) lep = std::max(lep, m.layout.lep);
+    // CTAs per SM only matter for patches of up to 384 element copies
+    const std::vector<int> cs = lep <= 384 ? ctas : std::vector<int>{saved[0].fim_ctas_per_sm};
+    for (int nc : cs) {
+      for (auto& m : b->members) {
+        m.prm.fim_ctas_per_sm = nc;
+        m.prm.flags &= ~(unsigned)LS_PROFILE;
+      }
+      b->solver.reset();
+      ls_status s = ls_batch_setup(b);
+      if (s == LS_PATCH_TOO_LARGE) break;
+      if (s != LS_OK) { restore(); return s; }
+      int done = 0;
+      std::string r = b->solver->run(1, nullptr, &done);  // warm-up (graph upload, caches)
+      if (!r.empty()) { restore(); return bsolver_status(b, r); }
+      b->solver->reset_stats();
+      r = b->solver->run(trial_steps, nullptr, &done);
+      if (!r.empty()) { restore(); return bsolver_status(b, r); }
+      lsgb::SolverStats t;
+      b->solver->stats(t);
+      const double ms = done > 0 ? t.ms_total / done : 0.0;
+      const double rate = t.ms_total > 0 ? (double)t.nb_vertex_updates / (t.ms_total / 1000.0) : 0.0;
+      trials.push_back({sz, nc, ms, rate});
+    }
+  }
+  b->solver.reset();
+  if (trials.empty()) {
+    restore();
+    return bfail(b, LS_PATCH_TOO_LARGE, "no candidate fits");
+  }
+  int best = 0;
+  for (int i = 1; i < (int)trials.size(); ++i)
+    if (trials[i].rate > trials[best].rate) best = i;
+  // leave the batch set up with the best candidate, every member at its phi0
+  restore();
+  if (trials[best].size > 0)
+    for (auto& m : b->members) {
+      ls_status s = relayout_member(b, m, trials[best].size);
+      if (s != LS_OK) return s;
+    }
+  for (auto& m : b->members) m.prm.fim_ctas_per_sm = trials[best].ctas;
+  ls_status s = ls_batch_setup(b);
+  if (rep) {
+    std::memset(rep, 0, sizeof(*rep));
+    rep->ntrials = std::min((int)trials.size(), LS_TUNE_MAX_TRIALS);
+    for (int i = 0; i < rep->ntrials; ++i) {
+      rep->trials[i].patch_size = trials[i].size;
+      rep->trials[i].fim_ctas_per_sm = trials[i].ctas;
+      rep->trials[i].ms_per_step = trials[i].ms;
+      rep->trials[i].updates_per_s = trials[i].rate;
+    }
+    rep->best = best;
+  }
+  return s;
 }
 
 ls_status ls_batch_solve(ls_batch* b, int nsteps, int* steps_done) {

@@ -73,7 +73,8 @@ EXPORTS = [
     "ls_batch_get_layout", "ls_autotune", "ls_mlp_create", "ls_mlp_destroy", "ls_mlp_last_error",
     "ls_mlp_num_params", "ls_mlp_set_params", "ls_mlp_get_params", "ls_mlp_predict", "ls_mlp_gradients",
     "ls_mlp_train", "ls_mlp_reserve_pairs", "ls_mlp_clear_pairs", "ls_mlp_num_pairs", "ls_mlp_train_pairs",
-    "ls_learn_collect", "ls_set_learned", "ls_batch_set_learned", "ls_mlp_eval_pairs", "ls_partition_graph", "ls_edge_cut",
+    "ls_learn_collect", "ls_set_learned", "ls_batch_set_learned", "ls_mlp_eval_pairs", "ls_batch_autotune",
+    "ls_partition_graph", "ls_edge_cut",
 ]
 
 class TuneTrial(ctypes.Structure):
@@ -140,6 +141,7 @@ def lib():
     L.ls_learn_collect.argtypes = [P, P, I, ctypes.POINTER(I)]
     L.ls_set_learned.argtypes = [P, P, ctypes.c_double, ctypes.c_double, I]
     L.ls_batch_set_learned.argtypes = [P, P, ctypes.c_double, ctypes.c_double, I]
+    L.ls_batch_autotune.argtypes = [P, I, V]
     L.ls_mlp_eval_pairs.argtypes = [P, ctypes.c_longlong, ctypes.c_longlong, V]
     L.ls_batch_create.argtypes = [ctypes.POINTER(P)]
     L.ls_batch_destroy.argtypes = [P]
@@ -477,6 +479,15 @@ class LevelSetBatch:
     def set_profile(self, on):
         self._check(lib().ls_batch_set_profile(self._b, 1 if on else 0), "batch set_profile")
 
+    def autotune(self, trial_steps=2):
+        """ls_batch_autotune: returns (trials, best index); the batch is left
+        set up with the best patch size and FIM setting."""
+        r = TuneReport()
+        self._check(lib().ls_batch_autotune(self._b, int(trial_steps), ctypes.byref(r)), "batch autotune")
+        trials = [dict(patch_size=t.patch_size, fim_ctas_per_sm=t.fim_ctas_per_sm, ms_per_step=t.ms_per_step,
+                       updates_per_s=t.updates_per_s) for t in r.trials[: r.ntrials]]
+        return trials, r.best
+
     def set_learned(self, mlp, margin=0.0, support_tol=0.0, reset_mode=0):
         self._check(lib().ls_batch_set_learned(self._b, mlp._m if mlp is not None else None, float(margin),
                                                float(support_tol), int(reset_mode)), "batch set_learned")
@@ -493,17 +504,22 @@ class LevelSetBatch:
 
 
 def from_workload(w, ref_compat=False, fp64_flagged=False, profile=False, setup=True, bit_exact=False, flags=0,
-                  **extra):
+                  structured_block=0, **extra):
     """LevelSet handle for a synth.workload() dictionary (mesh, partition,
-    phi0, velocity and the step parameters)."""
+    phi0, velocity and the step parameters).  structured_block > 0: the
+    library's structured partitioner with that block side on the lattice of
+    w["n"] + 1 vertices per side, instead of the workload's partition."""
     flags = flags | ((REF_COMPAT if ref_compat else 0) | (FP64_FLAGGED if fp64_flagged else 0) | (PROFILE if profile else 0)
              | (BITEXACT if bit_exact else 0))
     kind = {"advect": UPDATE_ADVECT, "curvature": UPDATE_CURVATURE, "none": UPDATE_NONE}[w["update"]]
+    if structured_block > 0:
+        extra = dict(extra, partition_type=1, side_lengths=w["n"] + 1, block_size=structured_block)
     p = default_params(num_steps=w["steps"], time_step=w["dt"], bandwidth=w["bandwidth"], update_kind=kind,
                        curv_coeff=1.0, flags=flags, **extra)
     ls = LevelSet(w["dim"] == 2, p)
     ls.set_mesh(w["xyz"], w["elems"])
-    ls.set_partition(w["npart"], w["nparts"])
+    if structured_block <= 0:
+        ls.set_partition(w["npart"], w["nparts"])
     ls.set_phi(w["phi0"])
     ls.set_velocity(w["vel"])
     if setup:

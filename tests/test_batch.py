@@ -98,3 +98,29 @@ def test_batch_curvature_members_and_profile_path():
     b.solve(3)
     for i, ref in enumerate(refs):
         assert np.array_equal(b.phi(i).view(np.uint32), ref.view(np.uint32)), i
+
+
+@pytest.mark.gpu
+def test_batch_autotune_leaves_best_setting():
+    # patch side and FIM setting tuned over the merged batch; the batch is
+    # left set up with the best at phi0 and steps as a batch built directly
+    # with those settings
+    ws = synth.workload_batch(seed=3, nmesh=4, nmin=8, nmax=16)
+
+    def batch(block, ctas=None):
+        b = lsgb300.LevelSetBatch()
+        for w in ws:
+            extra = {"fim_ctas_per_sm": ctas} if ctas else {}
+            b.add(lsgb300.from_workload(w, setup=False, structured_block=block, **extra))
+        return b
+
+    b = batch(3)
+    trials, best = b.autotune(1)
+    assert {t["patch_size"] for t in trials} == {2, 3, 4}
+    assert trials[best]["updates_per_s"] == max(t["updates_per_s"] for t in trials)
+    b.solve(3)
+    c = batch(trials[best]["patch_size"], trials[best]["fim_ctas_per_sm"])
+    c.setup()
+    c.solve(3)
+    for i in range(len(ws)):
+        assert np.array_equal(b.phi(i).view(np.uint32), c.phi(i).view(np.uint32)), i
