@@ -436,23 +436,25 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
 // PQ with f = Q - P, w = D - P and u = TQ - TP, the point P + l f with
 //   l = (f.w - |f x w| u / sqrt(|f|^2 - u^2)) / |f|^2
 // is where the characteristic through D meets the side (none when |u| >=
-// |f|).  For the interior, the in-plane gradient g solves the 2x2 Gram
-// system of AC, BC; the characteristic leaves the plane at
-// sqrt(1 - |g|^2), so the weight of A is the foot point's first barycentric
-// minus (hD / sqrt(1 - |g|^2)) times g's first coefficient (hD: D's height
-// over ABC).  The reference's quadratic in l1 has that root and its mirror
-// (the characteristic from the other side of the plane, foot point plus the
-// same offset); both are taken, with the weight of B from the reference's
-// own relation l2 = (s l1 + t) / (h + eps_h), so that its SMALLNUM offset
-// acts as in the reference (where h is small the offset moves the first
+// |f|), and its distance to D is |f x w| / sqrt(|f|^2 - u^2) (the same
+// quantity the reference evaluates at that point, without a square root of
+// its own).  For the interior, the in-plane gradient g solves the 2x2 Gram
+// system of AC, BC; the characteristic leaves the plane at sqrt(1 - |g|^2),
+// so the weight of A is the foot point's first barycentric minus (hD /
+// sqrt(1 - |g|^2)) times g's first coefficient (hD: D's height over ABC),
+// and the weight of B comes from the reference's own relation l2 = (s l1 +
+// t) / (h + eps_h), so that its SMALLNUM offset acts as in the reference; the
+// candidate is evaluated at that point as the reference does.  The
+// reference's quadratic also has the mirror root (the foot point plus the
+// same offset), taken too: where h is small the offset moves the first
 // root's point by far more than rounding, and the mirror's point can then be
-// the better one).  Each candidate is evaluated at its point as the
-// reference does.  The reference's discriminants q^2 - 4pr vanish
-// analytically whenever two arrival times along a side are equal, so in FP32
-// they come out as rounding noise of either sign (a negative one drops the
-// candidate: errors up to ~0.3 h); none of the quantities here cancel, and
-// the result stays within ~2e-5 h of the reference's solver run in FP64.
-// Invalid points come out as NaN or out of range and fail the range tests.
+// the better one.  The reference's discriminants q^2 -
+// 4pr vanish analytically whenever two arrival times along a side are equal,
+// so in FP32 they come out as rounding noise of either sign (a negative one
+// drops the candidate: errors up to ~0.3 h); none of the quantities here
+// cancel, and the result stays within ~5e-5 h of the reference's solver run
+// in FP64.  Invalid points come out as NaN or out of range and fail the
+// range tests.
 // Arguments as tet_solve, plus hD.
 __device__ __forceinline__ float tet_solve_wave(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
                                                 float BCBC, float BCCD, float CDCD, float hD, float eps_h, float LN) {
@@ -460,43 +462,38 @@ __device__ __forceinline__ float tet_solve_wave(float TA, float TB, float TC, fl
   // edges AD, BD, CD
   float best = fminf(fminf(TA + sqrtf((ACAC + ACCD) + (ACCD + CDCD)), TB + sqrtf((BCBC + BCCD) + (BCCD + CDCD))),
                      TC + sqrtf(CDCD));
-  {  // side BC: x = l2 B + (1 - l2) C (P = C, f = -BC, w = CD)
-    const float u = TB - TC;
-    const float l2 = (-BCCD - sqrtf(BCBC * CDCD - BCCD * BCCD) * u / sqrtf(BCBC - u * u)) / BCBC;
-    const float c = TB * l2 + TC * (1.f - l2) + sqrtf((l2 * BCBC + BCCD) * l2 + (l2 * BCCD + CDCD));
-    if (l2 >= 0.f && l2 <= 1.f) best = fminf(best, c);
-  }
-  {  // side AC: x = l1 A + (1 - l1) C (P = C, f = -AC, w = CD)
-    const float u = TA - TC;
-    const float l1 = (-ACCD - sqrtf(ACAC * CDCD - ACCD * ACCD) * u / sqrtf(ACAC - u * u)) / ACAC;
-    const float c = TA * l1 + TC * (1.f - l1) + sqrtf((l1 * ACAC + ACCD) * l1 + (l1 * ACCD + CDCD));
-    if (l1 >= 0.f && l1 <= 1.f) best = fminf(best, c);
-  }
-  {  // side AB: x = l1 A + (1 - l1) B (P = B, f = BC - AC, w = BC + CD)
-    const float u = TA - TB;
-    const float ff = (BCBC - ACBC) + (ACAC - ACBC);
-    const float fw = (BCBC + BCCD) - (ACBC + ACCD);
-    const float ww = (BCBC + BCCD) + (BCCD + CDCD);
-    const float l1 = (fw - sqrtf(ff * ww - fw * fw) * u / sqrtf(ff - u * u)) / ff;
-    const float l2 = 1.f - l1;
-    const float c = TA * l1 + TB * l2 +
-                    sqrtf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                          (l1 * ACCD + l2 * BCCD + CDCD));
-    if (l1 >= 0.f && l1 <= 1.f) best = fminf(best, c);
-  }
+  // sides: x = lam Q + (1 - lam) P with |Q - P|^2 = ff, (Q - P).(D - P) = fw,
+  // |D - P|^2 = ww and u = T_Q - T_P.  At the stationary point of
+  // T_P + lam u + |x - D| the distance is r = sqrt(ff ww - fw^2) /
+  // sqrt(ff - u^2) (no root when ff <= u^2: the rsqrt is then NaN or inf and
+  // the candidate is rejected) and lam = (fw - u r) / ff.
+  auto side = [&](float TP, float TQ, float ff, float fw, float ww) {
+    const float u = TQ - TP;
+    const float r = sqrtf(ff * ww - fw * fw) * rsqrtf(ff - u * u);
+    const float lam = (fw - u * r) / ff;
+    if (lam >= 0.f && lam <= 1.f) best = fminf(best, TP + lam * u + r);
+  };
+  side(TC, TB, BCBC, -BCCD, CDCD);  // side BC (P = C)
+  side(TC, TA, ACAC, -ACCD, CDCD);  // side AC (P = C)
+  side(TB, TA, (BCBC - ACBC) + (ACAC - ACBC), (BCBC + BCCD) - (ACBC + ACCD), (BCBC + BCCD) + (BCCD + CDCD));  // AB
   {  // interior of ABC: x = l1 A + l2 B + l3 C
     const float u1 = TA - TC, u2 = TB - TC;
     const float idet = 1.f / (ACAC * BCBC - ACBC * ACBC);
     const float g1 = (BCBC * u1 - ACBC * u2) * idet;  // in-plane gradient, coefficient of -AC
     const float g2 = (ACAC * u2 - ACBC * u1) * idet;  // and of -BC
     const float foot1 = (ACBC * BCCD - BCBC * ACCD) * idet;  // D's foot point, weight of A
-    const float dl = hD / sqrtf(1.f - (g1 * u1 + g2 * u2)) * g1;
+    // the point downhill of the foot point and its mirror uphill: the
+    // reference's SMALLNUM offset in l2 = (s l1 + t) / (h + eps_h) can move
+    // the first point out of the face where h is small, and the mirror's
+    // point is then the better one, as in the reference
+    const float dl = hD * rsqrtf(1.f - (g1 * u1 + g2 * u2)) * g1;
     const float TAC = TC - TA, TBC = TC - TB;
     const float s = TAC * ACBC - TBC * ACAC, t = TAC * BCCD - TBC * ACCD, h = -(TAC * BCBC - TBC * ACBC);
+    const float ih = 1.f / (h + eps_h);
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
       const float l1 = sgn ? foot1 + dl : foot1 - dl;
-      const float l2 = (s * l1 + t) / (h + eps_h);
+      const float l2 = (s * l1 + t) * ih;
       const float l3 = 1.f - l1 - l2;
       const float c = TA * l1 + TB * l2 + TC * l3 +
                       sqrtf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
