@@ -427,6 +427,11 @@ __device__ __forceinline__ float tet_solve_pred(float TA, float TB, float TC, fl
   return fminf(TD, fminf(FaceTBC, fminf(FaceTAB, FaceTAC)));
 }
 
+// l in [+0, 1] as one unsigned compare of the bits (negative values, -0.0
+// and NaN fail).  A candidate rejected for l = -0.0 sits at the side's end
+// point, where the edge candidate gives the same value.
+__device__ __forceinline__ bool in_unit(float l) { return __float_as_uint(l) <= 0x3f800000u; }
+
 // Tet update of D from the face ABC in FP32 without the quadratics (fast
 // build).  It returns the same quantity as tet_solve -- the least T_lin(x) +
 // |x - D| over the face, T_lin interpolating TA, TB, TC, with the reference's
@@ -471,7 +476,7 @@ __device__ __forceinline__ float tet_solve_wave(float TA, float TB, float TC, fl
     const float u = TQ - TP;
     const float r = sqrtf(ff * ww - fw * fw) * rsqrtf(ff - u * u);
     const float lam = (fw - u * r) / ff;
-    if (lam >= 0.f && lam <= 1.f) best = fminf(best, TP + lam * u + r);
+    if (in_unit(lam)) best = fminf(best, TP + lam * u + r);
   };
   side(TC, TB, BCBC, -BCCD, CDCD);  // side BC (P = C)
   side(TC, TA, ACAC, -ACCD, CDCD);  // side AC (P = C)
@@ -498,7 +503,7 @@ __device__ __forceinline__ float tet_solve_wave(float TA, float TB, float TC, fl
       const float c = TA * l1 + TB * l2 + TC * l3 +
                       sqrtf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
                             (l1 * ACCD + l2 * BCCD + CDCD));
-      if (l1 >= 0.f && l1 <= 1.f && l2 >= 0.f && l2 <= 1.f && l3 >= 0.f && l3 <= 1.f) best = fminf(best, c);
+      if (in_unit(l1) && in_unit(l2) && in_unit(l3)) best = fminf(best, c);
     }
   }
   return best;
