@@ -829,9 +829,9 @@ __device__ __forceinline__ bool slab_wait(unsigned bar, unsigned parity, bool gi
 // (ncap = the largest patch's copies, at most 2 x blockDim): copy values
 // float4 [ncap] (carried across sweeps), metric float4 [3][ncap] (11 terms,
 // copy-major), heights float4 [ncap], ghost results float4 [ncap],
-// connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k),
-// flags uchar [ncap] (changed vertices in bits 0-3, ghost vertices in bits
-// 4-7).
+// connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k);
+// each thread keeps its two copies' flags (changed and ghost vertices) in a
+// register.
 // The metric and height slabs come from the per-mesh geometry records
 // (k_geometry) by two bulk asynchronous copies that thread 0 issues at the
 // start of each patch; they land while the threads gather the values and
@@ -858,7 +858,6 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   float4* sR = sH + ncap;
   ushort4* sC = reinterpret_cast<ushort4*>(sR + ncap);
   unsigned short* sItem = reinterpret_cast<unsigned short*>(sC + ncap);
-  unsigned char* sF = reinterpret_cast<unsigned char*>(sItem + 4 * ncap);
   __shared__ unsigned s_min;
   __shared__ int s_n[2];  // listed solves, by sweep parity (reset one sweep ahead)
   __shared__ int s_li;    // list entry of the next patch
@@ -940,8 +939,11 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
           const unsigned b = __ballot_sync(0xffffffffu, sd);
           if ((i & 31) == 0) s_seed[i >> 5] = b;
         }
-      // the copies' connectivity and flags (the previous patch's last reads
-      // of these arrays came before its final barrier)
+      // the copies' connectivity (the previous patch's last reads of sC came
+      // before its final barrier) and flags, which only this thread reads:
+      // bits 8j .. 8j+3 the vertices of copy j that changed in the previous
+      // sweep (all on the first), bits 8j+4 .. 8j+7 its ghost vertices
+      unsigned flags = 0u;
   #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
@@ -950,7 +952,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
           sC[c] = cv;
           const unsigned ghost = (cv.x >= nvp ? 1u : 0u) | (cv.y >= nvp ? 2u : 0u) | (cv.z >= nvp ? 4u : 0u) |
                                  (cv.w >= nvp ? 8u : 0u);
-          sF[c] = (unsigned char)(0xFu | (ghost << 4));  // every input counts as changed on the first sweep
+          flags |= (0xFu | (ghost << 4)) << (8 * j);
         }
       }
       if (tid == 0) {
@@ -1001,7 +1003,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
           need[j] = 0u;
           // a copy none of whose values changed in the previous sweep lists
           // nothing: its flags are read first
-          const unsigned fl = c < nep ? sF[c] : 0u;
+          const unsigned fl = (flags >> (8 * j)) & 0xFFu;  // zero past nep
           if (fl & 0xFu) {
             const float4 tv = sTc[c];
             const float4 hv = sH[c];
@@ -1072,7 +1074,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
               if (c < nep) {
                 const float4 tv = sTc[c];
                 const float4 hv = sH[c];
-                const unsigned ghost = sF[c] >> 4;  // all four inputs count as changed
+                const unsigned ghost = (flags >> (8 * j + 4)) & 0xFu;  // all four inputs count as changed
                 const float LN = sp.largenum;
                 const float m012 = fminf(fminf(tv.x, tv.y), tv.z), m013 = fminf(fminf(tv.x, tv.y), tv.w);
                 const float m023 = fminf(fminf(tv.x, tv.z), tv.w), m123 = fminf(fminf(tv.y, tv.z), tv.w);
@@ -1117,7 +1119,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
             const unsigned chg = (nv.x != tv.x ? 1u : 0u) | (nv.y != tv.y ? 2u : 0u) | (nv.z != tv.z ? 4u : 0u) |
                                  (nv.w != tv.w ? 8u : 0u);
             sTc[c] = nv;
-            sF[c] = (unsigned char)((sF[c] & 0xF0u) | chg);
+            flags = (flags & ~(0xFu << (8 * j))) | (chg << (8 * j));
           }
         }
         // no barrier here: every thread refreshes only its own copies, and the
@@ -1976,9 +1978,9 @@ inline int compact_smem(const StepParams& sp, int maxt) {
 
 // dynamic shared memory of k_fim_pair for `ncap` copies: slab values, then
 // per copy 4 float4 records + metric (48 B) + connectivity (8 B) + listed
-// solves (8 B) + flags (1 B)
+// solves (8 B)
 inline int pair_smem(const StepParams& sp, int ncap) {
-  return (int)sizeof(float) * ((2 * sp.lvp + sp.lgp + 3) & ~3) + ncap * (16 * 3 + 48 + 8 + 8 + 1);
+  return (int)sizeof(float) * ((2 * sp.lvp + sp.lgp + 3) & ~3) + ncap * (16 * 3 + 48 + 8 + 8);
 }
 
 // The two-copies-per-thread kernels of this build: the planar-wave solver
