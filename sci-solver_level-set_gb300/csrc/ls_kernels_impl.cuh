@@ -830,8 +830,9 @@ __device__ __forceinline__ bool slab_wait(unsigned bar, unsigned parity, bool gi
 // float4 [ncap] (carried across sweeps), metric float4 [3][ncap] (11 terms,
 // copy-major), heights float4 [ncap], ghost results float4 [ncap],
 // connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k);
-// each thread keeps its two copies' flags (changed and ghost vertices) in a
-// register.
+// each thread keeps its two copies' flags (changed and ghost vertices) and
+// connectivity in registers as well (its own refresh reads them there; the
+// solves of other threads read the shared copy).
 // The metric and height slabs come from the per-mesh geometry records
 // (k_geometry) by two bulk asynchronous copies that thread 0 issues at the
 // start of each patch; they land while the threads gather the values and
@@ -978,7 +979,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
       for (int j = 0; j < 2; ++j) {
         const int c = tid + j * blockDim.x;
         if (c < nep) {
-          const ushort4 cv = sC[c];
+          const ushort4 cv = cvv[j];
           sTc[c] = make_float4(sT[cv.x], sT[cv.y], sT[cv.z], sT[cv.w]);
         }
       }
@@ -1109,7 +1110,7 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
           if (c < nep) {
             const float4 tv = sTc[c];
             const float4 rv = sR[c];
-            const ushort4 cv = sC[c];
+            const ushort4 cv = cvv[j];
             const unsigned nd = need[j];
             float4 nv;
             nv.x = cv.x < nvp ? sT[cv.x] : ((nd & 1u) ? rv.x : tv.x);
