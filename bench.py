@@ -35,7 +35,7 @@ METRIC = "narrowband vertex-updates/s (curvature flow, 128^3 jittered cube, 3 sp
 UNIT = "vertex-updates/s"
 # max |phi - phi_FP64| / h of the fast build over 3 steps of this workload,
 # measured by the GPU test named in ACCURACY
-C3_FAST_MAX_ERR_H = 9.39e-5
+C3_FAST_MAX_ERR_H = 9.44e-5
 
 
 # the two kernel builds and what the GPU tests establish about their accuracy

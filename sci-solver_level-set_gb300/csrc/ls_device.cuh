@@ -460,51 +460,71 @@ __device__ __forceinline__ bool in_unit(float l) { return __float_as_uint(l) <= 
 // cancel, and the result stays within ~5e-5 h of the reference's solver run
 // in FP64.  Invalid points come out as NaN or out of range and fail the
 // range tests.
+// Evaluation: sm_100 issues one FP32x2 instruction (add, multiply, fused
+// multiply-add, each lane rounded as the scalar operation) for two lanes, so
+// the independent halves run as pairs -- edges AD and BD, sides BC and AC
+// (both from C), the two interior roots -- with the square roots, side AB
+// and the interior's set-up per lane.
 // Arguments as tet_solve, plus hD.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
 __device__ __forceinline__ float tet_solve_wave(float TA, float TB, float TC, float ACAC, float ACBC, float ACCD,
                                                 float BCBC, float BCCD, float CDCD, float hD, float eps_h, float LN) {
   if (TA >= LN && TB >= LN && TC >= LN) return LN;
-  // edges AD, BD, CD
-  float best = fminf(fminf(TA + sqrtf((ACAC + ACCD) + (ACCD + CDCD)), TB + sqrtf((BCBC + BCCD) + (BCCD + CDCD))),
-                     TC + sqrtf(CDCD));
+  // edges AD, BD (lanes x, y) and CD
+  const float2 d2 = __fadd2_rn(__fadd2_rn(f2(ACAC, BCBC), f2(ACCD, BCCD)), __fadd2_rn(f2(ACCD, BCCD), f2(CDCD, CDCD)));
+  const float2 ed = __fadd2_rn(f2(TA, TB), f2(sqrtf(d2.x), sqrtf(d2.y)));
+  float best = fminf(fminf(ed.x, ed.y), TC + sqrtf(CDCD));
   // sides: x = lam Q + (1 - lam) P with |Q - P|^2 = ff, (Q - P).(D - P) = fw,
   // |D - P|^2 = ww and u = T_Q - T_P.  At the stationary point of
   // T_P + lam u + |x - D| the distance is r = sqrt(ff ww - fw^2) /
   // sqrt(ff - u^2) (no root when ff <= u^2: the rsqrt is then NaN or inf and
   // the candidate is rejected) and lam = (fw - u r) / ff.
-  auto side = [&](float TP, float TQ, float ff, float fw, float ww) {
-    const float u = TQ - TP;
+  {  // sides BC (lane x: P = C, Q = B) and AC (lane y: P = C, Q = A)
+    const float2 fw = f2(-BCCD, -ACCD), ff = f2(BCBC, ACAC);
+    const float2 u = __fadd2_rn(f2(TB, TA), f2(-TC, -TC));
+    const float2 G = __ffma2_rn(ff, f2(CDCD, CDCD), __fmul2_rn(fw, f2(BCCD, ACCD)));  // ff ww - fw^2
+    const float2 q = __ffma2_rn(u, f2(-u.x, -u.y), ff);                              // ff - u^2
+    const float2 r = __fmul2_rn(f2(sqrtf(G.x), sqrtf(G.y)), f2(rsqrtf(q.x), rsqrtf(q.y)));
+    const float2 lam = __fmul2_rn(__ffma2_rn(f2(-u.x, -u.y), r, fw), f2(1.f / ff.x, 1.f / ff.y));
+    const float2 c = __fadd2_rn(__ffma2_rn(lam, u, f2(TC, TC)), r);
+    if (in_unit(lam.x)) best = fminf(best, c.x);
+    if (in_unit(lam.y)) best = fminf(best, c.y);
+  }
+  {  // side AB (P = B, Q = A)
+    const float u = TA - TB;
+    const float ff = (BCBC - ACBC) + (ACAC - ACBC), fw = (BCBC + BCCD) - (ACBC + ACCD);
+    const float ww = (BCBC + BCCD) + (BCCD + CDCD);
     const float r = sqrtf(ff * ww - fw * fw) * rsqrtf(ff - u * u);
     const float lam = (fw - u * r) / ff;
-    if (in_unit(lam)) best = fminf(best, TP + lam * u + r);
-  };
-  side(TC, TB, BCBC, -BCCD, CDCD);  // side BC (P = C)
-  side(TC, TA, ACAC, -ACCD, CDCD);  // side AC (P = C)
-  side(TB, TA, (BCBC - ACBC) + (ACAC - ACBC), (BCBC + BCCD) - (ACBC + ACCD), (BCBC + BCCD) + (BCCD + CDCD));  // AB
+    if (in_unit(lam)) best = fminf(best, TB + lam * u + r);
+  }
   {  // interior of ABC: x = l1 A + l2 B + l3 C
     const float u1 = TA - TC, u2 = TB - TC;
     const float idet = 1.f / (ACAC * BCBC - ACBC * ACBC);
     const float g1 = (BCBC * u1 - ACBC * u2) * idet;  // in-plane gradient, coefficient of -AC
     const float g2 = (ACAC * u2 - ACBC * u1) * idet;  // and of -BC
     const float foot1 = (ACBC * BCCD - BCBC * ACCD) * idet;  // D's foot point, weight of A
-    // the point downhill of the foot point and its mirror uphill: the
-    // reference's SMALLNUM offset in l2 = (s l1 + t) / (h + eps_h) can move
-    // the first point out of the face where h is small, and the mirror's
-    // point is then the better one, as in the reference
+    // the point downhill of the foot point (lane x) and its mirror uphill
+    // (lane y): the reference's SMALLNUM offset in l2 = (s l1 + t) / (h +
+    // eps_h) can move the first point out of the face where h is small, and
+    // the mirror's point is then the better one, as in the reference
     const float dl = hD * rsqrtf(1.f - (g1 * u1 + g2 * u2)) * g1;
     const float TAC = TC - TA, TBC = TC - TB;
     const float s = TAC * ACBC - TBC * ACAC, t = TAC * BCCD - TBC * ACCD, h = -(TAC * BCBC - TBC * ACBC);
     const float ih = 1.f / (h + eps_h);
-#pragma unroll
-    for (int sgn = 0; sgn < 2; ++sgn) {
-      const float l1 = sgn ? foot1 + dl : foot1 - dl;
-      const float l2 = (s * l1 + t) * ih;
-      const float l3 = 1.f - l1 - l2;
-      const float c = TA * l1 + TB * l2 + TC * l3 +
-                      sqrtf((l1 * ACAC + l2 * ACBC + ACCD) * l1 + (l1 * ACBC + l2 * BCBC + BCCD) * l2 +
-                            (l1 * ACCD + l2 * BCCD + CDCD));
-      if (in_unit(l1) && in_unit(l2) && in_unit(l3)) best = fminf(best, c);
-    }
+    const float2 l1 = __fadd2_rn(f2(foot1, foot1), f2(-dl, dl));
+    const float2 l2 = __fmul2_rn(__ffma2_rn(f2(s, s), l1, f2(t, t)), f2(ih, ih));
+    const float2 l3 = __fadd2_rn(__fadd2_rn(f2(1.f, 1.f), f2(-l1.x, -l1.y)), f2(-l2.x, -l2.y));
+    // |x - D|^2 as the quadratic form of (l1, l2), and T_lin(x)
+    const float2 a1 = __ffma2_rn(l1, f2(ACAC, ACAC), __ffma2_rn(l2, f2(ACBC, ACBC), f2(ACCD, ACCD)));
+    const float2 a2 = __ffma2_rn(l1, f2(ACBC, ACBC), __ffma2_rn(l2, f2(BCBC, BCBC), f2(BCCD, BCCD)));
+    const float2 a3 = __ffma2_rn(l1, f2(ACCD, ACCD), __ffma2_rn(l2, f2(BCCD, BCCD), f2(CDCD, CDCD)));
+    const float2 Q = __ffma2_rn(a1, l1, __ffma2_rn(a2, l2, a3));
+    const float2 lin = __ffma2_rn(f2(TA, TA), l1, __ffma2_rn(f2(TB, TB), l2, __fmul2_rn(f2(TC, TC), l3)));
+    const float2 c = __fadd2_rn(lin, f2(sqrtf(Q.x), sqrtf(Q.y)));
+    if (in_unit(l1.x) && in_unit(l2.x) && in_unit(l3.x)) best = fminf(best, c.x);
+    if (in_unit(l1.y) && in_unit(l2.y) && in_unit(l3.y)) best = fminf(best, c.y);
   }
   return best;
 }
