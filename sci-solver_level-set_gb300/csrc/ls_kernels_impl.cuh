@@ -718,8 +718,8 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
   else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
   float r;
   if constexpr (SOLVER == kPairWave) {
-    const float4 hv = sH[cc];
-    const float hD = k == 0 ? hv.x : k == 1 ? hv.y : k == 2 ? hv.z : hv.w;
+    // the target's height: component k of the copy's record, loaded alone
+    const float hD = reinterpret_cast<const float*>(sH)[4 * cc + k];
     r = tet_solve_wave(a0, a1, a2, g0, g1, g2, g3, g4, g5, hD, sp.eps_h, sp.largenum);
   } else {
     bool d = false;
@@ -727,8 +727,8 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
                                                                 sp.eps_h64, sp.largenum, 0.f, d, own);
   }
   const float nw = fminf(own, r);
-  const ushort4 cv = sC[cc];
-  const int tk = k == 0 ? cv.x : k == 1 ? cv.y : k == 2 ? cv.z : cv.w;
+  // the target's slab index: component k of the copy's connectivity
+  const int tk = reinterpret_cast<const unsigned short*>(sC)[4 * cc + k];
   if (tk < nvp) atomicMin(reinterpret_cast<int*>(&sT[tk]), __float_as_int(nw));
   else reinterpret_cast<float*>(sR)[4 * cc + k] = nw;
 }
