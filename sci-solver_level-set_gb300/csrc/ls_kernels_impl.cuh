@@ -706,16 +706,19 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
                                            const ushort4* sC, float* sT, float4* sR, int nvp, const StepParams& sp) {
   const int cc = code >> 2, k = code & 3;
   const float4 tv = sTc[cc];
-  const float4 m0 = sM[3 * cc], m1 = sM[3 * cc + 1], m2 = sM[3 * cc + 2];
   const float TA = tv.x, TB = tv.y, TC = tv.z, TD = tv.w;
-  const float ACAC = m0.x, ACBC = m0.y, ACCD = m0.z, BCBC = m0.w, BCCD = m1.x, CDCD = m1.y;
-  const float ADAD = m1.z, ADBD = m1.w, ADCD = m2.x, BDBD = m2.y, CDBD = m2.z;
+  // the six metric terms of solve k (k_geometry's record: floats 0-5 for
+  // solves 0, 1, 3, floats 6-11 for solve 2), v0 .. v5 = ACAC ACBC ACCD BCBC
+  // BCCD CDCD, or ADAD ADBD ADCD BDBD CDBD CDCD
+  const float2* mp = reinterpret_cast<const float2*>(sM) + 6 * cc + (k == 2 ? 3 : 0);
+  const float2 p0 = mp[0], p1 = mp[1], p2 = mp[2];
+  const float v0 = p0.x, v1 = p0.y, v2 = p1.x, v3 = p1.y, v4 = p2.x, v5 = p2.y;
   // the permuted arguments of solve k (solve_copy's four calls)
   float a0, a1, a2, g0, g1, g2, g3, g4, g5, own;
-  if (k == 3) { a0 = TA; a1 = TB; a2 = TC; g0 = ACAC; g1 = ACBC; g2 = ACCD; g3 = BCBC; g4 = BCCD; g5 = CDCD; own = TD; }
-  else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = BCBC; g1 = -BCCD; g2 = -ACBC; g3 = CDCD; g4 = ACCD; g5 = ACAC; own = TA; }
-  else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = ACAC; g1 = -ACCD; g2 = -ACBC; g3 = CDCD; g4 = BCCD; g5 = BCBC; own = TB; }
-  else { a0 = TA; a1 = TB; a2 = TD; g0 = ADAD; g1 = ADBD; g2 = -ADCD; g3 = BDBD; g4 = -CDBD; g5 = CDCD; own = TC; }
+  if (k == 3) { a0 = TA; a1 = TB; a2 = TC; g0 = v0; g1 = v1; g2 = v2; g3 = v3; g4 = v4; g5 = v5; own = TD; }
+  else if (k == 0) { a0 = TB; a1 = TD; a2 = TC; g0 = v3; g1 = -v4; g2 = -v1; g3 = v5; g4 = v2; g5 = v0; own = TA; }
+  else if (k == 1) { a0 = TA; a1 = TD; a2 = TC; g0 = v0; g1 = -v2; g2 = -v1; g3 = v5; g4 = v4; g5 = v3; own = TB; }
+  else { a0 = TA; a1 = TB; a2 = TD; g0 = v0; g1 = v1; g2 = -v2; g3 = v3; g4 = -v4; g5 = v5; own = TC; }
   float r;
   if constexpr (SOLVER == kPairWave) {
     // the target's height: component k of the copy's record, loaded alone
@@ -734,9 +737,11 @@ __device__ __forceinline__ void pair_solve(int code, const float4* sTc, const fl
 }
 
 // Per-copy geometry of the two-copies-per-thread sweep, computed once per
-// mesh: the copy's metric terms (copy_metric) as three float4 and the heights
-// of its four vertices over their opposite faces, the same expressions the
-// one-copy kernels evaluate per visit.
+// mesh: the copy's metric terms (copy_metric) as three float4 -- ACAC ACBC
+// ACCD BCBC | BCCD CDCD ADAD ADBD | ADCD BDBD CDBD CDCD, so that floats 0-5
+// hold the six terms solves 0, 1 and 3 permute and floats 6-11 the six of
+// solve 2 -- and the heights of its four vertices over their opposite faces,
+// the same expressions the one-copy kernels evaluate per visit.
 __global__ void k_geometry(DevMesh m, float4* gm, float4* gh) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < m.full; c += stride) {
@@ -744,7 +749,7 @@ __global__ void k_geometry(DevMesh m, float4* gm, float4* gh) {
     copy_metric<4>(m, c, Mt);
     gm[3 * c] = make_float4(Mt[0], Mt[1], Mt[2], Mt[3]);
     gm[3 * c + 1] = make_float4(Mt[4], Mt[5], Mt[6], Mt[7]);
-    gm[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], 0.f);
+    gm[3 * c + 2] = make_float4(Mt[8], Mt[9], Mt[10], Mt[5]);
     const float ACAC = Mt[0], ACBC = Mt[1], ACCD = Mt[2], BCBC = Mt[3], BCCD = Mt[4], CDCD = Mt[5];
     const float ADAD = Mt[6], ADBD = Mt[7], BDBD = Mt[9];
     const float det3 = ACAC * (BCBC * CDCD - BCCD * BCCD) - ACBC * (ACBC * CDCD - BCCD * ACCD) +
