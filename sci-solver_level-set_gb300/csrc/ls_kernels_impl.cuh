@@ -1222,17 +1222,19 @@ __device__ __forceinline__ void schedule_pass(const DevMesh& m, const DevState& 
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int w = (vb * blockDim.x + threadIdx.x) >> 5; w < count; w += nwarps) {
     const int p = list[w] & ~kPrevisited;
+    // the patch's records, loaded together (none depends on the copy-back)
     const int vs = m.vert_off[p], ve = m.vert_off[p + 1];
+    const int con = s.bcon[p];
+    const float bmin = s.bmin[p];
+    const int a = m.padj_off[p], b = m.padj_off[p + 1];
     for (int v = vs + lane; v < ve; v += 32)
       if (!s.seed[v]) s.DT[v] = s.DT_out[v];
-    const int con = s.bcon[p];
     if (!con) {
       if (lane == 0) {
         const int pos = atomicAdd(&s.counts[nxt], 1);
         nlist[pos] = p;
       }
-    } else if (s.bmin[p] < patch_par(m, sp, p).bw) {
-      const int a = m.padj_off[p], b = m.padj_off[p + 1];
+    } else if (bmin < patch_par(m, sp, p).bw) {
       for (int j0 = a; j0 < b; j0 += 32) {
         const int j = j0 + lane;
         int q = -1;
