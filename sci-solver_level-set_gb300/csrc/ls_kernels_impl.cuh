@@ -893,10 +893,11 @@ __device__ __forceinline__ void fim_pair_pass(const DevMesh& m, const DevState& 
   // first entry by CTA index, later ones drawn from a counter (draw_patch)
   int* next = s.sched + (CHECK ? 1 : 0);
   // visits run by the checks that activate them only pay when the check
-  // launch is throughput bound (two patches or more per resident CTA): on
-  // fewer patches they add a visit's length to the iteration, while the next
-  // sweep launch still waits for the patches that stayed active
-  const bool early = CHECK && sp.niter > 1 && count >= 2 * (int)gridDim.x;
+  // launch is throughput bound (four checks or more per resident CTA, the
+  // best of 1, 2, 4 and 8 measured at 128^3): on fewer patches they add a
+  // visit's length to the iteration, while the next sweep launch still waits
+  // for the patches that stayed active
+  const bool early = CHECK && sp.niter > 1 && count >= 4 * (int)gridDim.x;
   // the owned vertices' seed flags are kept in shared memory when every patch
   // fits the mask (read by the check's verdict and the copy-out)
   const bool seed_mask = sp.lvp <= 32 * kSeedMaskWords;

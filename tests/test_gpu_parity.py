@@ -173,12 +173,12 @@ def test_two_copies_per_thread_sweep_equals_one_copy_sweep(name, n, update):
 
 
 def test_visits_run_by_checks_change_nothing():
-    # on a mesh whose neighbour-check launches hold two or more patches per
+    # on a mesh whose neighbour-check launches hold four or more patches per
     # resident CTA, the two-copies-per-thread kernel runs the visits of the
     # patches its checks activate in the same launch; the one-copy kernel
     # visits them in the next iteration: same bits, same work counters
-    w = synth.workload("c3", n=96)
-    nsteps = 3
+    w = synth.workload("c3", n=128)
+    nsteps = 2
     runs = {}
     for ctas in (3, 5):
         ls = lsgb300.from_workload(w, fim_ctas_per_sm=ctas)
