@@ -51,8 +51,9 @@ struct DevMesh {
   const float4* mesh_par;
   // per copy, precomputed once per mesh for the two-copies-per-thread tet
   // sweep (null otherwise): the 11 metric terms of copy_metric as three
-  // float4 (geo_m[3c .. 3c+2], last lane a second copy of CDCD) and the heights of A, B, C, D
-  // over their opposite faces (geo_h[c]); a patch's copies are contiguous,
+  // float4 (geo_m[3c .. 3c+2], last lane a second copy of CDCD) and the
+  // heights of A, B, C, D over their opposite faces (geo_h[c]); a patch's
+  // copies are contiguous,
   // so its records are two contiguous slabs, staged by bulk asynchronous
   // copies
   const float4* geo_m;

@@ -832,8 +832,8 @@ __device__ __forceinline__ bool slab_wait(unsigned bar, unsigned parity, bool gi
 // kernel fits three): the CTA barriers between the listing, solve and
 // refresh phases then leave fewer issue slots idle.  Shared memory per CTA
 // (ncap = the largest patch's copies, at most 2 x blockDim): copy values
-// float4 [ncap] (carried across sweeps), metric float4 [3][ncap] (11 terms,
-// copy-major), heights float4 [ncap], ghost results float4 [ncap],
+// float4 [ncap] (carried across sweeps), metric float4 [3][ncap] (11 terms
+// and a second CDCD, copy-major), heights float4 [ncap], ghost results float4 [ncap],
 // connectivity ushort4 [ncap], listed solves ushort [4 ncap] (copy << 2 | k);
 // each thread keeps its two copies' flags (changed and ghost vertices) and
 // connectivity in registers as well (its own refresh reads them there; the
