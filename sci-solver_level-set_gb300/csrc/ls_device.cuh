@@ -53,9 +53,8 @@ struct DevMesh {
   // sweep (null otherwise): the 11 metric terms of copy_metric as three
   // float4 (geo_m[3c .. 3c+2], last lane a second copy of CDCD) and the
   // heights of A, B, C, D over their opposite faces (geo_h[c]); a patch's
-  // copies are contiguous,
-  // so its records are two contiguous slabs, staged by bulk asynchronous
-  // copies
+  // copies are contiguous, so its records are two contiguous slabs, staged
+  // by bulk asynchronous copies
   const float4* geo_m;
   const float4* geo_h;
 };
